@@ -1,0 +1,46 @@
+"""quantit_gb300: QuantiT's block-sparse tensor hot path on GB300 (sm_103a).
+
+The package mirrors the Python API of QuantiT (module ``quantit``) for the
+accelerated path -- ``btensor`` contraction, sector SVD / eigh with truncation,
+and two-site DMRG -- over the C-ABI of libqtt_gb300.so (include/qtt_gb300.h).
+All arithmetic runs in CUDA kernels; nothing falls back to the CPU.
+"""
+from . import algorithms, conserved, linalg, networks
+from ._lib import LIB_PATH, ensure_init, lib
+from .tensor import btensor, dot_all, from_blocks, tensordot, tensorgdot, tensorgdot_
+
+__all__ = ["algorithms", "conserved", "linalg", "networks", "btensor", "dot_all", "from_blocks", "tensordot",
+           "tensorgdot", "tensorgdot_", "LIB_PATH", "ensure_init", "lib", "stats", "set_gemm_mode"]
+
+
+def set_gemm_mode(mode):
+    """Block-GEMM precision: 'f64' (drop-in), 'tf32x3' or 'bf16x3'."""
+    from ._lib import call
+    call("qtt_set_gemm_mode", algorithms.GEMM_MODES[mode] if isinstance(mode, str) else int(mode))
+
+
+class stats:
+    """Per-kernel-class device time (CUDA events) and algorithmic work."""
+    KINDS = {"gemm": 0, "permute": 1, "svd": 2, "elementwise": 3, "pack": 4}
+
+    @staticmethod
+    def enable(on=True):
+        from ._lib import call
+        call("qtt_stats_enable", int(bool(on)))
+
+    @staticmethod
+    def reset():
+        from ._lib import call
+        call("qtt_stats_reset")
+
+    @staticmethod
+    def get(kind):
+        import ctypes as C
+        from ._lib import call
+        ms, work, n = C.c_double(), C.c_double(), C.c_int64()
+        call("qtt_stats_get", stats.KINDS[kind], C.byref(ms), C.byref(work), C.byref(n))
+        return {"ms": ms.value, "work": work.value, "launches": n.value}
+
+    @staticmethod
+    def launches():
+        return int(lib().qtt_launch_count())

@@ -1,0 +1,66 @@
+"""Builds libqtt_gb300.so in-tree with nvcc for sm_103a (GB300).
+
+Every translation unit under csrc/ is compiled in parallel; the objects go to
+quantit_gb300/_build/ and the shared library to quantit_gb300/libqtt_gb300.so.
+Run: python -m quantit_gb300.build   (or call build()).
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libqtt_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _compile(nvcc, src, verbose_ptxas=False):
+    obj = os.path.join(OUT, os.path.basename(src) + ".o")
+    if os.path.exists(obj) and os.path.getmtime(obj) > max(
+            os.path.getmtime(src), *[os.path.getmtime(os.path.join(CSRC, h)) for h in os.listdir(CSRC) if h.endswith(".h")],
+            os.path.getmtime(os.path.join(HERE, "..", "include", "qtt_gb300.h"))):
+        return obj, ""
+    cmd = [nvcc, *ARCH, *FLAGS, "-c", src, "-o", obj]
+    if src.endswith(".cpp"):
+        cmd[1:1] = ["-x", "cu"]
+    if verbose_ptxas:
+        cmd += ["-Xptxas", "-v"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
+    return obj, r.stderr
+
+
+def build(verbose=False, ptxas=False):
+    nvcc = _nvcc()
+    os.makedirs(OUT, exist_ok=True)
+    srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+        results = list(ex.map(lambda s: _compile(nvcc, s, ptxas), srcs))
+    objs = [o for o, _ in results]
+    if ptxas or verbose:
+        for (o, log) in results:
+            if log:
+                print(os.path.basename(o), log, file=sys.stderr)
+    newest = max(os.path.getmtime(o) for o in objs)
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcuda"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, ptxas="--ptxas" in sys.argv))

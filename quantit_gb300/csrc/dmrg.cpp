@@ -1,0 +1,216 @@
+// Two-site DMRG on the device (sources/dmrg.cpp).
+//
+// The bond update keeps every Lanczos scalar on the device: the inner products
+// a0, <r|r>, a1 are written by the dot kernels, b = sqrt(<r|r>) and the closed
+// form 2x2 Ritz step (eig2x2Mat_impl, :544-572) run in one-thread kernels, and
+// the axpby kernels read their coefficients from device memory.  The only host
+// synchronisation of a bond update is the read-back of the singular values for
+// the truncation threshold, which also brings back the bond energy.
+#include <chrono>
+#include <cmath>
+
+#include "contract.h"
+#include "dmrg.h"
+#include "kernels.h"
+#include "ops_util.h"
+#include "qtt_core.h"
+
+namespace qtt {
+
+BT compute_2sites_hamil(const BT &wl, const BT &wr) {
+    return permute(tensordot(wl, wr, {2}, {0}), {0, 1, 3, 4, 2, 5});
+}
+
+BT hamil2site_times_state(const BT &state, const BT &hamil, const BT &L, const BT &R) {
+    BT out = tensordot(L, state, {0}, {0});
+    out = tensordot(out, hamil, {0, 2, 3}, {0, 4, 5});
+    return tensordot(out, R, {1, 4}, {0, 1});
+}
+
+BT compute_left_env(const BT &W, const BT &A, const BT &L) {
+    BT out = tensordot(L, A, {0}, {0});
+    out = tensordot(out, W, {0, 2}, {0, 3});
+    return tensordot(out, conj(A), {0, 2}, {0, 1});
+}
+
+BT compute_right_env(const BT &W, const BT &A, const BT &R) {
+    BT out = tensordot(R, A, {0}, {2});
+    out = tensordot(out, W, {0, 3}, {2, 3});
+    return tensordot(out, conj(A), {3, 0}, {1, 2});
+}
+
+void eig2x2(double a0, double a1, double b, double &E, double &o, double &n) {
+    double crit = std::sqrt((a0 - a1) * (a0 - a1) + 4.0 * (b * b));
+    E = (a0 + a1 - crit) / 2.0;
+    double delt = E - a1;
+    o = std::sqrt(delt / (-crit));
+    bool zero_o = ((o + E) == E) || std::isnan(o);
+    n = (b * o) / delt;
+    if (zero_o) {
+        n = 1.0;
+        o = 0.0;
+    }
+    if (std::isnan(o) || std::isnan(n)) fail(ERR_LOGIC, "nan found in output tensor");
+}
+
+// scal layout: [0] a0, [1] b, [2] a1, [3] E, [4] o, [5] n, [6] nan flag
+LanczosOut one_step_lanczos_dev(const BT &state, const BT &hamil, const BT &L, const BT &R, double *scal,
+                                DevScratch &scr) {
+    BT psi = hamil2site_times_state(state, hamil, L, R);
+    dot_all_dev(psi, state, scal + 0, scr);
+    psi = add_scaled_dev(psi, state, coef_host(1.0), Coef{-1.0, scal + 0, 0, 0, 0.0});
+    dot_all_dev(psi, psi, scal + 1, scr);
+    launch_sqrt(scal + 1);
+    psi = scale_dev(psi, Coef{1.0, scal + 1, 1, 0, 1e-15});
+    BT hpsi = hamil2site_times_state(psi, hamil, L, R);
+    dot_all_dev(psi, hpsi, scal + 2, scr);
+    LanczosOut o;
+    o.psi = psi;
+    return o;
+}
+
+LanczosHost one_step_lanczos(const BT &state, const BT &hamil, const BT &L, const BT &R) {
+    DevScratch scr;
+    double *scal = scr.get(8);
+    LanczosOut r = one_step_lanczos_dev(state, hamil, L, R, scal, scr);
+    double h[3];
+    cuda_check(cudaMemcpyAsync(h, scal, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx().stream), "cudaMemcpyAsync");
+    cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+    LanczosHost o;
+    o.psi = r.psi;
+    o.a0 = h[0];
+    o.b = h[1];
+    o.a1 = h[2];
+    return o;
+}
+
+namespace {
+BT trivial_edge(const BT &st, int sleg, const BT &w, int wleg) {
+    // all-ones rank-3 edge (generate_env_impl, dmrg.cpp:371-391; edge_shape_prep :335-345)
+    BT e;
+    e.g = st.g;
+    e.dt = F64;
+    e.rank = 3;
+    auto adS = st.addrs(), adW = w.addrs();
+    auto add_leg = [&](const BT &t, const std::vector<int64_t> &ad, int leg, bool inv) {
+        e.sbd.push_back(t.sbd[leg]);
+        for (int64_t s = 0; s < t.sbd[leg]; ++s) {
+            e.ssz.push_back(t.ssz[ad[leg] + s]);
+            Charge q = t.cv[ad[leg] + s];
+            e.cv.push_back(inv ? qinv(q, t.g) : q);
+        }
+    };
+    add_leg(st, adS, sleg, true);
+    add_leg(w, adW, wleg, true);
+    add_leg(st, adS, sleg, false);
+    Charge q;
+    for (auto &c : e.cv) q = qadd(q, c, e.g);
+    e.sel = q;
+    std::vector<int64_t> idx;
+    for (int64_t a = 0; a < e.sbd[0]; ++a)
+        for (int64_t b = 0; b < e.sbd[1]; ++b)
+            for (int64_t c = 0; c < e.sbd[2]; ++c) {
+                int64_t ix[3] = {a, e.sbd[0] + b, e.sbd[0] + e.sbd[1] + c};
+                Charge s = qadd(qadd(e.cv[ix[0]], e.cv[ix[1]], e.g), e.cv[ix[2]], e.g);
+                if (qeq(s, e.sel, e.g)) {
+                    idx.push_back(a);
+                    idx.push_back(b);
+                    idx.push_back(c);
+                }
+            }
+    set_blocks(e, int64_t(idx.size() / 3), idx.data(), true, nullptr, false);
+    // ones
+    std::vector<double> ones(e.nnz, 1.0);
+    if (e.nnz) {
+        cuda_check(cudaMemcpyAsync(e.data(), ones.data(), ones.size() * 8, cudaMemcpyHostToDevice, ctx().stream),
+                   "cudaMemcpyAsync(edge)");
+        cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+    }
+    return e;
+}
+}  // namespace
+
+double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, const DmrgOpts &opt, DmrgLog log,
+            void *user) {
+    const int64_t L = int64_t(mpo.size());
+    if (L < 2 || int64_t(mps.size()) != L) fail(ERR_INVALID_ARGUMENT, "MPO and MPS need the same length >= 2");
+    const int saved_mode = gemm_mode();
+    set_gemm_mode(opt.gemm_mode);
+    struct ModeGuard {
+        int m;
+        ~ModeGuard() { set_gemm_mode(m); }
+    } guard{saved_mode};
+    // compute_2sitesHamil (dmrg.cpp:504-515)
+    std::vector<BT> h2(L - 1);
+    for (int64_t i = 0; i < L - 1; ++i) h2[i] = compute_2sites_hamil(mpo[i], mpo[i + 1]);
+    // generate_env (dmrg.cpp:371-409); env[i+1] holds Env[i]
+    int64_t oc = oc_io;
+    std::vector<BT> env(L + 2);
+    env[0] = trivial_edge(mps[0], 0, mpo[0], 0);
+    env[L + 1] = trivial_edge(mps[L - 1], 2, mpo[L - 1], 2);
+    for (int64_t i = 0; i < oc; ++i) env[i + 1] = compute_left_env(mpo[i], mps[i], env[i]);
+    for (int64_t i = L - 1; i > oc; --i) env[i + 1] = compute_right_env(mpo[i], mps[i], env[i + 2]);
+    // dmrg_impl (dmrg.cpp:219-273)
+    double E0 = 100000.0;
+    int64_t init_pos = oc;
+    const int64_t nh = L - 1;
+    const int64_t n_step = nh - 1 + (nh == 1);
+    int step = (oc == 0) ? 1 : -1;
+    if (nh == 1) step = 0;
+    if (oc == L - 1) {
+        --init_pos;
+        --oc;
+    }
+    double *hscal = nullptr;
+    cuda_check(cudaMallocHost(&hscal, 8 * sizeof(double)), "cudaMallocHost");
+    struct HostFree {
+        double *p;
+        ~HostFree() { cudaFreeHost(p); }
+    } hf{hscal};
+    for (int64_t it = 0; it < opt.maximum_iterations; ++it) {
+        auto t0 = std::chrono::steady_clock::now();
+        double E = 0.0;
+        for (int64_t k = 0; k < 2 * n_step; ++k) {
+            const bool forward = step == 1;
+            DevScratch scr;
+            double *scal = scr.get(8);
+            BT theta = tensordot(mps[oc], mps[oc + 1], {2}, {0});
+            LanczosOut lz = one_step_lanczos_dev(theta, h2[oc], env[oc], env[oc + 3], scal, scr);
+            launch_eig2x2(scal);
+            BT upd = add_scaled_dev(theta, lz.psi, Coef{1.0, scal + 4, 0, 0, 0.0}, Coef{1.0, scal + 5, 0, 0, 0.0});
+            cuda_check(cudaMemcpyAsync(hscal, scal, 7 * sizeof(double), cudaMemcpyDeviceToHost, ctx().stream),
+                       "cudaMemcpyAsync(scalars)");
+            SVDOut f = svd_truncated(upd, 2, opt.cutoff, opt.minimum_bond, opt.maximum_bond, 2.0);  // syncs
+            if (hscal[6] != 0.0) fail(ERR_LOGIC, "nan found in output tensor");
+            E = hscal[3];
+            // d /= sqrt(sum(d.pow(2)))  (dmrg.cpp:188)
+            launch_normalize(static_cast<double *>(f.d.data()), f.d.nnz, nullptr);
+            if (forward) {
+                mps[oc] = f.U;
+                mps[oc + 1] = permute(conj(mul_lastleg(f.V, f.d)), {2, 0, 1});
+                env[oc + 1] = compute_left_env(mpo[oc], mps[oc], env[oc]);
+            } else {
+                mps[oc] = mul_lastleg(f.U, f.d);
+                mps[oc + 1] = permute(conj(f.V), {2, 0, 1});
+                env[oc + 2] = compute_right_env(mpo[oc + 1], mps[oc + 1], env[oc + 3]);
+            }
+            oc += step;
+            if (oc == 0 || oc == L - 2) step = -step;
+        }
+        cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+        double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (log) log(user, it, E, secs);
+        double prev = E0;
+        E0 = E;
+        if (!(std::fabs((E0 - prev) / E0) > opt.convergence_criterion)) break;
+    }
+    if (oc != init_pos) {
+        if (oc != init_pos - 1 && init_pos != L - 1)
+            fail(ERR_RUNTIME, "the orthogonality center finished somewhere surprising! final oc: " +
+                                  std::to_string(oc) + ". original oc: " + std::to_string(init_pos));
+    }
+    oc_io = oc;
+    return E0;
+}
+
+}  // namespace qtt

@@ -1,0 +1,39 @@
+// DMRG building blocks and driver.
+#pragma once
+#include <vector>
+
+#include "ops_util.h"
+#include "qtt_core.h"
+
+namespace qtt {
+
+struct DmrgOpts {
+    double cutoff = 1e-6;
+    double convergence_criterion = 1e-5;
+    int64_t maximum_bond = INT64_MAX;
+    int64_t minimum_bond = 4;
+    int64_t maximum_iterations = 1000;
+    int gemm_mode = GEMM_F64;
+};
+typedef void (*DmrgLog)(void *user, int64_t sweep, double energy, double seconds);
+
+struct LanczosOut {
+    BT psi;
+};
+struct LanczosHost {
+    BT psi;
+    double a0 = 0, a1 = 0, b = 0;
+};
+
+BT compute_2sites_hamil(const BT &wl, const BT &wr);
+BT hamil2site_times_state(const BT &state, const BT &hamil, const BT &L, const BT &R);
+BT compute_left_env(const BT &W, const BT &A, const BT &L);
+BT compute_right_env(const BT &W, const BT &A, const BT &R);
+void eig2x2(double a0, double a1, double b, double &E, double &o, double &n);
+LanczosOut one_step_lanczos_dev(const BT &state, const BT &hamil, const BT &L, const BT &R, double *scal,
+                                DevScratch &scr);
+LanczosHost one_step_lanczos(const BT &state, const BT &hamil, const BT &L, const BT &R);
+double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc, const DmrgOpts &opt, DmrgLog log,
+            void *user);
+
+}  // namespace qtt

@@ -1,0 +1,153 @@
+// Launch wrappers between the host layer and the CUDA kernels.  All tables are
+// device pointers prepared by the host planner (uploaded through the staging
+// ring); all launches go to the current context stream.
+#pragma once
+#include <atomic>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace qtt {
+
+// Work over many variable-length segments is cut into chunks of at most
+// CHUNK elements that never straddle a segment; one CTA handles one chunk.
+constexpr int CHUNK = 2048;
+struct Chunk {
+    int32_t seg;
+    int32_t len;
+    int64_t start;  // element offset inside the segment
+};
+
+// ------------------------------------------------------------ permute / copy
+// Segment = one block: dst[dst_off + e] = src[src_off + sum_d idx_d(e) * stride[d]]
+// where idx(e) is the row-major multi-index of e over dims[0..rank).
+struct PermEntry {
+    int64_t src_off, dst_off;
+    int32_t rank, pad;
+    int64_t dims[8];
+    int64_t stride[8];
+};
+void launch_permute(const void *src, void *dst, const PermEntry *entries, const Chunk *chunks, int64_t nchunks,
+                    int elem_bytes);
+
+// ------------------------------------------------------------ grouped GEMM
+// Output block o: C[o] (M x N row-major at c_off) = alpha * sum_{p in [p0,p1)} A_p B_p
+//                                                   + beta * Cadd (at add_off, when add_off >= 0).
+// A_p is M x K: row-major at a_off when a_t == 0, stored K x M row-major when a_t == 1.
+// B_p is K x N: row-major at b_off when b_t == 0, stored N x K row-major when b_t == 1.
+struct GemmPair {
+    int64_t a_off, b_off;
+    int32_t K;
+    int32_t pad;
+};
+struct GemmOut {
+    int64_t c_off, add_off;
+    int32_t M, N;
+    int32_t p0, p1;
+};
+struct GemmTile {
+    int32_t out, m0, n0, pad;
+};
+struct GemmArgs {
+    const double *A;
+    const double *B;
+    double *C;
+    const double *Cadd;
+    const GemmPair *pairs;
+    const GemmOut *outs;
+    const GemmTile *tiles;
+    int32_t ntiles;
+    int32_t a_t, b_t;
+    double alpha, beta;
+};
+void launch_gemm_f64(const GemmArgs &a);
+// Split-precision tensor-core variant (tcgen05); mode as GemmMode.
+void launch_gemm_tc(const GemmArgs &a, int mode);
+int gemm_tile_m(int mode);
+int gemm_tile_n(int mode);
+
+// ------------------------------------------------------------ elementwise
+// A coefficient: mult * (dev ? f(*dev) : 1) with f(x) = x, or f(x) = 1/x when
+// invert is set and |x| >= guard (f(x) = 1 below the guard).
+struct Coef {
+    double mult;
+    const double *dev;
+    int32_t invert;
+    int32_t pad;
+    double guard;
+};
+inline Coef coef_host(double v) { return Coef{v, nullptr, 0, 0, 0.0}; }
+// Segment: out[out_off + i] = ca * a[a_off + i] + cb * b[b_off + i]; an offset of -1 reads 0.
+struct AxpbySeg {
+    int64_t a_off, b_off, out_off;
+};
+void launch_axpby(const double *a, const double *b, double *out, const AxpbySeg *segs, const Chunk *chunks,
+                  int64_t nchunks, Coef ca, Coef cb);
+// Segment: sum_i a[a_off + i] * b[b_off + i]; partial sums per chunk then a fixed-order
+// reduction into *out (device), so the result is deterministic.
+struct DotSeg {
+    int64_t a_off, b_off;
+};
+void launch_dot(const double *a, const double *b, const DotSeg *segs, const Chunk *chunks, int64_t nchunks,
+                double *partials, double *out);
+// Segment: out[out_off + e] = u[u_off + e] * d[d_off + (e % L)]
+struct LastLegSeg {
+    int64_t u_off, d_off, out_off, L;
+};
+void launch_mul_lastleg(const double *u, const double *d, double *out, const LastLegSeg *segs, const Chunk *chunks,
+                        int64_t nchunks);
+// x[0..n) *= 1/sqrt(sum x^2)   (d /= sqrt(sum(d.pow(2))), sources/dmrg.cpp:188)
+void launch_normalize(double *x, int64_t n, double *scratch);
+void launch_convert(const void *src, void *dst, int64_t n, int src_f64, int dst_f64);
+
+// ------------------------------------------------------------ sector decompositions
+// Sector s: m x n matrix A; the work matrix W (p x q, column-major, p >= q) is A when
+// m >= n, A^T otherwise.  Offsets are element offsets into the work, rotation,
+// left-vector, right-vector and value buffers.
+struct SectorDesc {
+    int64_t w_off, rot_off, u_off, v_off, s_off;
+    int32_t m, n, p, q;
+    int32_t trans;  // 1 when W = A^T
+    int32_t mode;   // 0: svd, 1: eigh (symmetric input, shifted to positive definite)
+    double shift;   // eigh: diagonal shift added before the sweeps
+};
+// Segment = one input block (rows x cols at src_off) placed at rows [r0, r0+rows),
+// cols [c0, c0+cols) of sector `sector`.
+struct PackEntry {
+    int64_t src_off;
+    int32_t sector, rows, cols, r0, c0, pad;
+};
+void launch_zero(double *p, int64_t n);
+void launch_pack(const double *src, double *work, const PackEntry *e, const Chunk *chunks, int64_t nchunks,
+                 const SectorDesc *sec);
+// eigh: symmetrise W from one triangle, then shift the diagonal by the sector's
+// Frobenius norm (written back into sec[s].shift) so the matrix is positive definite.
+void launch_eigh_prepare(double *work, SectorDesc *sec, int nsec, int upper);
+// Batched one-sided Jacobi over all sectors in one cooperative launch.
+// slot_start[nsec+1]: prefix sums of the pairs each sector contributes per step
+// ((q + q%2)/2); max_steps_per_sweep = max over sectors of (q + q%2 - 1).
+// sweeps_out[s] receives the number of sweeps sector s used; flags holds
+// 2*nsec+1 ints of scratch.
+void launch_jacobi(double *work, double *rot, const SectorDesc *sec, const int *slot_start, int nsec,
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags);
+// Column norms, sort (descending for svd, ascending eigenvalues for eigh),
+// normalisation and completion of null columns; writes U (m x k), V (n x k)
+// column-major and s (k) per sector, k = min(m, n).
+// The work buffer is reused as scratch.  max_q: largest q over the sectors.
+void launch_finish(double *work, const double *rot, double *U, double *V, double *s, const SectorDesc *sec,
+                   int nsec, int max_q);
+// Segment = one output block (rows x k row-major at dst_off) from a column-major
+// (ld x *) sector matrix at src_off: dst[i*k + j] = src[src_off + (r0 + i) + j*ld].
+struct ScatterEntry {
+    int64_t src_off, dst_off;
+    int32_t ld, r0, k, pad;
+};
+void launch_scatter(const double *src, double *dst, const ScatterEntry *e, const Chunk *chunks, int64_t nchunks);
+
+// ------------------------------------------------------------ 2x2 Ritz step on device
+// s[0]=a0, s[1]=b, s[2]=a1  ->  s[3]=E, s[4]=o, s[5]=n, s[6]=nan flag
+// (eig2x2Mat_impl, sources/dmrg.cpp:544-572)
+void launch_eig2x2(double *s);
+void launch_sqrt(double *x);
+
+}  // namespace qtt
