@@ -192,6 +192,9 @@ int qtt_stats_reset(void);
 int qtt_stats_get(int kind, double *ms, double *work, int64_t *launches);
 /* Number of kernels this library launched since load. */
 int64_t qtt_launch_count(void);
+/* Jacobi sweeps each sector needed in the most recent decomposition (synchronises);
+ * *n receives the sector count, up to cap values are written to out. */
+int qtt_last_svd_sweeps(int32_t *out, int32_t cap, int32_t *n);
 
 #ifdef __cplusplus
 }

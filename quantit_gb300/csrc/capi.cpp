@@ -424,5 +424,12 @@ int qtt_stats_get(int kind, double *ms, double *work, int64_t *launches) {
     return guarded([&] { qtt::stats_get(kind, ms, work, launches); });
 }
 int64_t qtt_launch_count(void) { return qtt::launch_count(); }
+int qtt_last_svd_sweeps(int32_t *out, int32_t cap, int32_t *n) {
+    return guarded([&] {
+        auto v = qtt::last_svd_sweeps();
+        if (n) *n = int32_t(v.size());
+        for (int32_t i = 0; i < cap && i < int32_t(v.size()); ++i) out[i] = v[i];
+    });
+}
 
 }  // extern "C"

@@ -198,6 +198,7 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
             if (oc == 0 || oc == L - 2) step = -step;
         }
         cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+        tc_error_raise();
         double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (log) log(user, it, E, secs);
         double prev = E0;

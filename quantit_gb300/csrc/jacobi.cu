@@ -43,21 +43,25 @@ struct JacobiParams {
     int nsec;
     int max_sweeps;
     int64_t max_steps;
-    int *sweeps;  // per sector
-    int *flags;   // [0, nsec): rotated this sweep, [nsec, 2nsec): done, [2nsec]: number done
+    int *sweeps;   // per sector (written at the end)
+    int *rotated;  // nsec * max_sweeps flags, zero on entry: a rotation happened in (sector, sweep)
 };
 
+// One grid barrier per step.  Every CTA keeps its own copy of the per-sector
+// sweep / done state in shared memory and updates it identically after each
+// barrier from the rotation flags, so no second barrier is needed to publish it.
 __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
     cg::grid_group grid = cg::this_grid();
+    extern __shared__ int jsh[];
+    const int nsec = P.nsec;
+    int *done = jsh;            // nsec
+    int *sweep = jsh + nsec;    // nsec
+    __shared__ int ndone;
     const int lane = threadIdx.x & 31;
     const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
     const int64_t gt = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t nt = int64_t(gridDim.x) * blockDim.x;
-    const int nsec = P.nsec;
-    int *rotated = P.flags;
-    int *done = P.flags + nsec;
-    int *ndone = P.flags + 2 * nsec;
     const int total_slots = P.slot_start[nsec];
 
     // rotation matrices start as identity; sectors with < 2 columns are done at once
@@ -66,21 +70,17 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
         const int64_t qq = int64_t(sd.q) * sd.q;
         for (int64_t e = gt; e < qq; e += nt) P.rot[sd.rot_off + e] = (e % (sd.q + 1) == 0) ? 1.0 : 0.0;
     }
-    if (gt < nsec) {
-        rotated[gt] = 0;
-        P.sweeps[gt] = 0;
-        done[gt] = (P.secs[gt].q < 2) ? 1 : 0;
-    }
-    grid.sync();
-    if (gt == 0) {
-        int c = 0;
-        for (int s = 0; s < nsec; ++s) c += done[s];
-        *ndone = c;
+    if (threadIdx.x == 0) ndone = 0;
+    __syncthreads();
+    for (int s = threadIdx.x; s < nsec; s += blockDim.x) {
+        done[s] = (P.secs[s].q < 2) ? 1 : 0;
+        sweep[s] = 0;
+        if (done[s]) atomicAdd(&ndone, 1);
     }
     grid.sync();
 
     for (int64_t step = 0; step < P.max_steps; ++step) {
-        if (*(volatile int *)ndone >= nsec) break;
+        if (ndone >= nsec) break;
         for (int64_t slot = gw; slot < total_slots; slot += nw) {
             // sector of this slot
             int lo = 0, hi = nsec - 1;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
                     hi = mid - 1;
             }
             const int s = lo;
-            if (((volatile int *)done)[s]) continue;
+            if (done[s]) continue;
             const SectorDesc sd = P.secs[s];
             const int qp = sd.q + (sd.q & 1);
             const int k = int(step % (qp - 1));
@@ -138,26 +138,28 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
                 va[r] = c * x - sn * y;
                 vb[r] = sn * x + c * y;
             }
-            if (lane == 0) rotated[s] = 1;
+            if (lane == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
         }
         grid.sync();
-        if (blockIdx.x == 0) {
-            for (int s = threadIdx.x; s < nsec; s += blockDim.x) {
-                if (done[s]) continue;
-                const int q = P.secs[s].q;
-                const int qp = q + (q & 1);
-                if ((step + 1) % (qp - 1) == 0) {
-                    P.sweeps[s] += 1;
-                    if (!rotated[s] || P.sweeps[s] >= P.max_sweeps) {
-                        done[s] = 1;
-                        atomicAdd(ndone, 1);
-                    }
-                    rotated[s] = 0;
+        // end-of-sweep bookkeeping, identical in every CTA
+        for (int s = threadIdx.x; s < nsec; s += blockDim.x) {
+            if (done[s]) continue;
+            const int q = P.secs[s].q;
+            const int qp = q + (q & 1);
+            if ((step + 1) % (qp - 1) == 0) {
+                const int sw = sweep[s];
+                const bool rot = ((volatile int *)P.rotated)[int64_t(s) * P.max_sweeps + sw] != 0;
+                sweep[s] = sw + 1;
+                if (!rot || sw + 1 >= P.max_sweeps) {
+                    done[s] = 1;
+                    atomicAdd(&ndone, 1);
                 }
             }
         }
-        grid.sync();
+        __syncthreads();
     }
+    if (blockIdx.x == 0)
+        for (int s = threadIdx.x; s < nsec; s += blockDim.x) P.sweeps[s] = sweep[s];
 }
 
 // One CTA per sector: column norms, ordering, normalisation, completion.
@@ -271,15 +273,21 @@ __global__ void __launch_bounds__(1024) k_finish(double *__restrict__ work, cons
 }  // namespace
 
 void launch_jacobi(double *work, double *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                          int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags) {
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags) {
     if (nsec <= 0) return;
-    static int nsm = 0, per_sm = 0;
+    static int nsm = 0;
     if (!nsm) {
         int dev = ctx().device;
         cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
-        cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi, JT, 0), "occupancy");
-        per_sm = std::max(1, std::min(per_sm, 4));
+        cuda_check(cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
+                   "Jacobi smem attribute");
     }
+    if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
+    const size_t smem = size_t(2 * nsec) * sizeof(int);
+    int per_sm = 0;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi, JT, smem), "occupancy");
+    per_sm = std::max(1, std::min(per_sm, 4));
+    cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), ctx().stream), "memset flags");
     JacobiParams P;
     P.work = work;
     P.rot = rot;
@@ -289,10 +297,10 @@ void launch_jacobi(double *work, double *rot, const SectorDesc *sec, const int *
     P.max_sweeps = max_sweeps;
     P.max_steps = int64_t(max_sweeps) * std::max(1, max_steps_per_sweep) + 1;
     P.sweeps = sweeps_out;
-    P.flags = flags;
+    P.rotated = flags;
     void *args[] = {&P};
     dim3 grid(nsm * per_sm), block(JT);
-    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi, grid, block, args, 0, ctx().stream),
+    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi, grid, block, args, smem, ctx().stream),
                "cooperative Jacobi launch");
     count_launch();
 }

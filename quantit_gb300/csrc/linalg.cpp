@@ -137,6 +137,16 @@ BT single_leg(const BT &like, const std::vector<int64_t> &sizes, const std::vect
     return o;
 }
 
+// sweep counts of the most recent decomposition (diagnostics)
+struct LastSweeps {
+    BufPtr buf;
+    int n = 0;
+};
+LastSweeps &last_sweeps() {
+    static LastSweeps l;
+    return l;
+}
+
 struct Decomp {
     std::vector<Sector> secs;
     std::vector<SectorDesc> desc;  // one per (sector, batch element)
@@ -223,14 +233,17 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
                     int64_t(chunks.size()), dsec);
     }
     if (mode == 1) launch_eigh_prepare(W, dsec, nsec, upper);
-    auto ibuf = dev_alloc(size_t(3 * nsec + 2) * sizeof(int));
+    const int max_sweeps = 80;
+    auto ibuf = dev_alloc(size_t(nsec) * (max_sweeps + 1) * sizeof(int));
     int *sweeps = static_cast<int *>(ibuf->p);
     int *flags = sweeps + nsec;
+    last_sweeps() = {ibuf, nsec};
     double est = 0;
     for (auto &d : D.desc) est += 8.0 * double(d.q) * double(d.q) * (6.0 * d.p + 4.0 * d.q);
     {
         StatScope sc(ST_SVD, est);
-        launch_jacobi(W, static_cast<double *>(D.rot->p), dsec, upload_vec(slots), nsec, max_steps, 40, sweeps, flags);
+        launch_jacobi(W, static_cast<double *>(D.rot->p), dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps,
+                      flags);
         launch_finish(W, static_cast<double *>(D.rot->p), static_cast<double *>(D.U->p),
                       static_cast<double *>(D.V->p), static_cast<double *>(D.S->p), dsec, nsec, max_q);
     }
@@ -367,6 +380,17 @@ SVDOut svd(const BT &t) {
 }
 
 // svd(A, split), btensor_linalg.cpp:503-534
+std::vector<int> last_svd_sweeps() {
+    LastSweeps &l = last_sweeps();
+    std::vector<int> out(l.n);
+    if (l.n && l.buf) {
+        cuda_check(cudaMemcpyAsync(out.data(), l.buf->p, size_t(l.n) * sizeof(int), cudaMemcpyDeviceToHost,
+                                   ctx().stream), "cudaMemcpyAsync(sweeps)");
+        cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+    }
+    return out;
+}
+
 SVDOut svd_split(const BT &t, int64_t split) {
     if (split < 1 || split >= t.rank) fail(ERR_INVALID_ARGUMENT, "split must leave legs on both sides");
     BT rt = reshape(t, {split});
@@ -449,6 +473,7 @@ SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, dou
                    "cudaMemcpyAsync(d)");
         cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
     }
+    tc_error_raise();
     std::vector<double> vd(vals.begin(), vals.end());
     // per-block value ranges in stored order
     std::vector<int64_t> bstart(d.nblocks()), blen(d.nblocks());

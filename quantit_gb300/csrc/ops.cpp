@@ -343,6 +343,7 @@ double dot_all(const BT &a, const BT &b) {
     double h = 0;
     cuda_check(cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, ctx().stream), "cudaMemcpyAsync");
     cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+    tc_error_raise();
     return h;
 }
 

@@ -282,6 +282,7 @@ struct EighOut {
 };
 EighOut eigh(const BT &t, bool upper);
 EighOut eigh_split(const BT &t, int64_t split);
+std::vector<int> last_svd_sweeps();  // Jacobi sweeps per sector of the last decomposition
 
 // ---------------------------------------------------------------- precision of block GEMMs
 enum GemmMode : int {
@@ -291,6 +292,12 @@ enum GemmMode : int {
 };
 void set_gemm_mode(int mode);
 int gemm_mode();
+// Non-zero when a tensor-core kernel gave up on a bounded wait since the last
+// check (synchronises the device; read and cleared).
+int tc_error_check();
+inline void tc_error_raise() {
+    if (int e = tc_error_check()) fail(ERR_RUNTIME, "tensor-core GEMM: bounded wait expired (code " + std::to_string(e) + ")");
+}
 
 // ---------------------------------------------------------------- timing statistics
 // Per-kernel-class device time measured with CUDA events on the launching stream,

@@ -1,0 +1,89 @@
+"""The split-TF32 tcgen05 grouped GEMM (pytest -m gpu).
+
+Tolerance: TF32x3 keeps hi*hi + hi*lo + lo*hi with FP32 accumulation, about FP32
+accuracy, so a block product agrees with the FP64 result to 2e-6 relative to the
+block's largest magnitude (checked against the oracle)."""
+import numpy as np
+import pytest
+
+import quantit_gb300 as q
+from oracle import qtt_oracle as o
+from tests._convert import same_structure, to_device
+from tests.test_library_cpu import _contractible_pair
+
+pytestmark = pytest.mark.gpu
+TOL = 2e-6
+
+
+@pytest.fixture
+def tf32x3():
+    q.set_gemm_mode("tf32x3")
+    yield
+    q.set_gemm_mode("f64")
+
+
+def _check(got, want, tol=TOL):
+    assert same_structure(got, want)
+    blocks = got.blocks()
+    assert [k for k, _ in blocks] == [k for k, _ in want.blocks]
+    for (k, a), (_, b) in zip(blocks, want.blocks):
+        scale = max(float(np.max(np.abs(b))) if b.size else 0.0, 1e-300)
+        err = float(np.max(np.abs(a - b))) if b.size else 0.0
+        assert err <= tol * scale, (k, err, scale)
+
+
+def test_tc_gemm_random_layouts(tf32x3):
+    rng = np.random.default_rng(21)
+    n = 0
+    for trial in range(600):
+        if n >= 25:
+            break
+        ra, rb = int(rng.integers(1, 5)), int(rng.integers(1, 5))
+        nc = int(rng.integers(0, min(ra, rb) + 1))
+        A, B, dA, dB = _contractible_pair(rng, (0,), ra, rb, nc)
+        if not A.blocks or not B.blocks:
+            continue
+        _check(to_device(A).tensordot(to_device(B), (dA, dB)), o.tensordot(A, B, dA, dB))
+        n += 1
+    assert n >= 10
+
+
+@pytest.mark.parametrize("sizes", [(40, 70, 33), (130, 257, 129), (300, 190, 200)])
+def test_tc_gemm_large_blocks(tf32x3, sizes):
+    a, b, c = sizes
+    rng = np.random.default_rng(22)
+    A = o.btensor([[(a, -1), (b, 0), (c, 1)], [(1, -1), (1, 1)], [(1, -1), (1, 1)], [(c, -2), (b, 0), (a, 2)]],
+                  [0], (0,))
+    A = o.randn_like(A, rng)
+    B = o.btensor([[(c, 2), (b, 0), (a, -2)], [(1, 1), (1, -1)], [(b, 1), (c, -1)]], [0], (0,))
+    B = o.randn_like(B, rng)
+    for dA, dB in (([3, 2], [0, 1]), ([3], [0]), ([0], [2])):
+        try:
+            want = o.tensordot(A, B, dA, dB)
+        except o.ContractionError:
+            continue
+        _check(to_device(A).tensordot(to_device(B), (dA, dB)), want, tol=5e-6)
+
+
+def test_tc_gemm_tensorgdot_epilogue(tf32x3):
+    rng = np.random.default_rng(23)
+    A, B, dA, dB = _contractible_pair(rng, (0,), 3, 3, 1)
+    while not A.blocks or not B.blocks:
+        A, B, dA, dB = _contractible_pair(rng, (0,), 3, 3, 1)
+    C = o.tensordot(A, B, dA, dB)
+    add = o.randn_like(C.empty_like(), rng)
+    _check(q.tensorgdot(to_device(add), to_device(A), to_device(B), dA, dB, beta=0.5, alpha=2.0),
+           o.tensorgdot(add, A, B, dA, dB, beta=0.5, alpha=2.0), tol=5e-6)
+
+
+def test_mixed_dmrg_energy_close_to_fp64():
+    L, D = 12, 32
+    mpo = o.heisenberg_mpo(L)
+    mps = o.right_canonicalize(o.random_mps(L, D, [1, -1], 0, np.random.default_rng(5)))
+    dmpo = q.networks.bMPO([to_device(t) for t in mpo])
+    res = {}
+    for mode in ("f64", "tf32x3"):
+        dmps = q.networks.bMPS([to_device(t) for t in mps], 0)
+        res[mode] = q.algorithms.dmrg(dmpo, dmps, q.algorithms.dmrg_options(
+            cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4, maximum_iterations=4, gemm=mode))
+    assert abs(res["tf32x3"] - res["f64"]) / L < 1e-8, res
