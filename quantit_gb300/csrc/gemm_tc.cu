@@ -275,6 +275,8 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(GemmArgs g, int *er
     }
 }
 
+std::atomic<bool> g_tc_used{false};  // a tensor-core launch happened since the last error check
+
 int *err_word() {
     static int *p = nullptr;
     if (!p) {
@@ -305,9 +307,6 @@ void launch_gemm_tc(const GemmArgs &a, int mode) {
 }
 
 // Non-zero when a tensor-core kernel hit a bounded wait (read and cleared; synchronises).
-namespace {
-std::atomic<bool> g_tc_used{false};
-}
 int tc_error_check() {
     if (!g_tc_used.exchange(false)) return 0;
     int h = 0;
