@@ -156,7 +156,8 @@ typedef struct {
     int64_t minimum_bond;          /* default 4 */
     int64_t maximum_iterations;    /* sweeps (default 1000) */
     int32_t gemm_mode;             /* QTT_GEMM_* for the matvecs and environment updates */
-    int32_t reserved;
+    int32_t final_energy_fp64;     /* mixed gemm_mode: return the FP64 <psi|H|psi>/<psi|psi> of the
+                                      final state instead of the last Ritz value (default 1) */
 } qtt_dmrg_options;
 /* dmrg_options defaults (include/dmrg_options.h:15-58) */
 void qtt_dmrg_options_default(qtt_dmrg_options *opt);
@@ -182,6 +183,10 @@ int qtt_compute_right_env(qtt_bt W, qtt_bt A, qtt_bt Renv, qtt_bt *out);
  * *oc is the orthogonality centre in and out; *E0 the final energy. */
 int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
              qtt_dmrg_log_fn log_fn, void *log_user, double *E0);
+
+/* <psi|H|psi> and <psi|psi> of an MPS against an MPO, contracted in FP64
+ * (contract(bMPS, bMPS, bMPO) and contract(bMPS, bMPS), include/MPT.h; sources/MPT.cpp:211-290). */
+int qtt_mps_energy(int32_t L, const qtt_bt *mpo, const qtt_bt *mps, double *energy, double *norm2);
 
 /* ------------------------------------------------------------------ measurement */
 /* Per-kernel-class device time (CUDA events on the launching stream) and

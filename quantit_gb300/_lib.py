@@ -73,6 +73,7 @@ SIGNATURES = {
     "qtt_compute_left_env": (C.c_int, [bt, bt, bt, P(bt)]),
     "qtt_compute_right_env": (C.c_int, [bt, bt, bt, P(bt)]),
     "qtt_dmrg": (C.c_int, [i32, P(bt), P(bt), P(i64), vp, vp, vp, P(f64)]),
+    "qtt_mps_energy": (C.c_int, [i32, P(bt), P(bt), P(f64), P(f64)]),
     "qtt_stats_enable": (C.c_int, [C.c_int]),
     "qtt_stats_reset": (C.c_int, []),
     "qtt_stats_get": (C.c_int, [C.c_int, P(f64), P(f64), P(i64)]),
@@ -83,7 +84,7 @@ SIGNATURES = {
 
 class DmrgOptionsC(C.Structure):
     _fields_ = [("cutoff", f64), ("convergence_criterion", f64), ("maximum_bond", i64), ("minimum_bond", i64),
-                ("maximum_iterations", i64), ("gemm_mode", i32), ("reserved", i32)]
+                ("maximum_iterations", i64), ("gemm_mode", i32), ("final_energy_fp64", i32)]
 
 
 LOG_FN = C.CFUNCTYPE(None, vp, i64, f64, f64)

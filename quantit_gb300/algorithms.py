@@ -12,13 +12,15 @@ class dmrg_options:
     """dmrg_options (include/dmrg_options.h:15-58) plus the block-GEMM precision."""
 
     def __init__(self, *, cutoff=1e-6, convergence_criterion=1e-5, max_bond=SIZE_MAX, min_bond=4,
-                 maximum_iterations=1000, gemm="f64"):
+                 maximum_iterations=1000, gemm="f64", final_energy_fp64=True):
         self.cutoff = cutoff
         self.convergence_criterion = convergence_criterion
         self.maximum_bond = max_bond
         self.minimum_bond = min_bond
         self.maximum_iterations = maximum_iterations
         self.gemm = gemm
+        # mixed precision: return the FP64 <psi|H|psi>/<psi|psi> of the final state
+        self.final_energy_fp64 = final_energy_fp64
 
     def _c(self):
         o = _lib.DmrgOptionsC()
@@ -28,6 +30,7 @@ class dmrg_options:
         o.minimum_bond = int(self.minimum_bond)
         o.maximum_iterations = int(self.maximum_iterations)
         o.gemm_mode = GEMM_MODES[self.gemm] if isinstance(self.gemm, str) else int(self.gemm)
+        o.final_energy_fp64 = int(bool(self.final_energy_fp64))
         return o
 
 
@@ -70,6 +73,16 @@ def dmrg(mpo, mps, options=None, logger=None):
     if hasattr(mps, "orthogonality_center"):
         mps.orthogonality_center = oc.value
     return E.value
+
+
+def mps_energy(mpo, mps):
+    """(<psi|H|psi>, <psi|psi>) contracted in FP64 (contract(bMPS, bMPS, bMPO))."""
+    L = len(mpo)
+    mpo_h = (C.c_void_p * L)(*[t._h.value for t in mpo])
+    mps_h = (C.c_void_p * L)(*[t._h.value for t in mps])
+    e, n = C.c_double(), C.c_double()
+    _lib.call("qtt_mps_energy", L, mpo_h, mps_h, C.byref(e), C.byref(n))
+    return e.value, n.value
 
 
 def hamil2site_times_state(state, hamil, Lenv, Renv):

@@ -343,7 +343,7 @@ void qtt_dmrg_options_default(qtt_dmrg_options *o) {
     o->minimum_bond = 4;
     o->maximum_iterations = 1000;
     o->gemm_mode = QTT_GEMM_F64;
-    o->reserved = 0;
+    o->final_energy_fp64 = 1;
 }
 int qtt_compute_2sites_hamil(qtt_bt wl, qtt_bt wr, qtt_bt *out) {
     return guarded([&] {
@@ -408,9 +408,22 @@ int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_d
             o.minimum_bond = opt->minimum_bond;
             o.maximum_iterations = opt->maximum_iterations;
             o.gemm_mode = opt->gemm_mode;
+            o.final_energy_fp64 = opt->final_energy_fp64;
         }
         *E0 = qtt::dmrg(W, S, *oc, o, log_fn, log_user);
         for (int i = 0; i < L; ++i) mps[i] = wrap(std::move(S[i]));
+    });
+}
+
+int qtt_mps_energy(int32_t L, const qtt_bt *mpo, const qtt_bt *mps, double *energy, double *norm2) {
+    return guarded([&] {
+        out_check(energy);
+        std::vector<qtt::BT> W(L), S(L);
+        for (int i = 0; i < L; ++i) {
+            W[i] = T(mpo[i]);
+            S[i] = T(mps[i]);
+        }
+        *energy = qtt::mps_energy(W, S, norm2);
     });
 }
 

@@ -130,6 +130,40 @@ BT trivial_edge(const BT &st, int sleg, const BT &w, int wleg) {
 }
 }  // namespace
 
+namespace {
+double sum_all(const BT &t) {
+    if (t.nnz == 0) return 0.0;
+    std::vector<double> h(t.nnz);
+    cuda_check(cudaMemcpyAsync(h.data(), t.data(), size_t(t.nnz) * 8, cudaMemcpyDeviceToHost, ctx().stream),
+               "cudaMemcpyAsync(scalar)");
+    cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+    double s = 0.0;
+    for (double x : h) s += x;
+    return s;
+}
+}  // namespace
+
+// <psi|H|psi> and <psi|psi> by contracting the chain from the left in FP64
+// (contract(bMPS, bMPS, bMPO) and contract(bMPS, bMPS), sources/MPT.cpp:211-290).
+double mps_energy(const std::vector<BT> &mpo, const std::vector<BT> &mps, double *norm2) {
+    const int64_t L = int64_t(mpo.size());
+    if (L < 1 || int64_t(mps.size()) != L) fail(ERR_INVALID_ARGUMENT, "MPO and MPS need the same length");
+    const int saved = gemm_mode();
+    set_gemm_mode(GEMM_F64);
+    struct G {
+        int m;
+        ~G() { set_gemm_mode(m); }
+    } guard{saved};
+    BT env = trivial_edge(mps[0], 0, mpo[0], 0);
+    for (int64_t i = 0; i < L; ++i) env = compute_left_env(mpo[i], mps[i], env);
+    const double e = sum_all(env);
+    BT n = tensordot(mps[0], conj(mps[0]), {0, 1}, {0, 1});
+    for (int64_t i = 1; i < L; ++i) n = tensordot(tensordot(n, mps[i], {0}, {0}), conj(mps[i]), {0, 1}, {0, 1});
+    const double nn = sum_all(n);
+    if (norm2) *norm2 = nn;
+    return e;
+}
+
 double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, const DmrgOpts &opt, DmrgLog log,
             void *user) {
     const int64_t L = int64_t(mpo.size());
@@ -211,6 +245,13 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
                                   std::to_string(oc) + ". original oc: " + std::to_string(init_pos));
     }
     oc_io = oc;
+    if (opt.gemm_mode != GEMM_F64 && opt.final_energy_fp64) {
+        // the mixed path's Ritz values carry the FP32-level noise of its block
+        // GEMMs; the variational energy of its final state, reduced in FP64, does not
+        double n2 = 1.0;
+        const double e = mps_energy(mpo, mps, &n2);
+        E0 = e / n2;
+    }
     return E0;
 }
 

@@ -14,6 +14,7 @@ struct DmrgOpts {
     int64_t minimum_bond = 4;
     int64_t maximum_iterations = 1000;
     int gemm_mode = GEMM_F64;
+    int final_energy_fp64 = 1;  // mixed modes: return the FP64 <psi|H|psi>/<psi|psi> of the final state
 };
 typedef void (*DmrgLog)(void *user, int64_t sweep, double energy, double seconds);
 
@@ -35,5 +36,6 @@ LanczosOut one_step_lanczos_dev(const BT &state, const BT &hamil, const BT &L, c
 LanczosHost one_step_lanczos(const BT &state, const BT &hamil, const BT &L, const BT &R);
 double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc, const DmrgOpts &opt, DmrgLog log,
             void *user);
+double mps_energy(const std::vector<BT> &mpo, const std::vector<BT> &mps, double *norm2);
 
 }  // namespace qtt

@@ -1,11 +1,16 @@
 // Batched per-sector SVD / symmetric eigendecomposition by one-sided (Hestenes)
-// Jacobi in FP64.  All sectors of a decomposition run in ONE cooperative launch:
-// at every step each sector contributes its round-robin set of disjoint column
+// Jacobi.  All sectors of a decomposition run in ONE cooperative launch: at
+// every step each sector contributes its round-robin set of disjoint column
 // pairs, every warp in the grid takes pairs from the combined list, and a grid
 // barrier closes the step.  This replaces the per-sector LAPACK calls of
 // btensor_linalg.cpp:483 (torch::svd) and :354 (linalg eigh).
 //
-// The loop is bounded: at most max_sweeps sweeps per sector.
+// The work type T is double for the plain FP64 path and float for the mixed
+// path (FP32 runs on GB300's CUDA cores at 64x the FP64 rate; the mixed DMRG
+// reports its energy from an FP64 contraction of the final state, which is
+// second order in the SVD's orthogonality error).  Outputs are always FP64.
+//
+// Every loop is bounded: at most max_sweeps sweeps per sector.
 #include <cooperative_groups.h>
 
 #include "kernels.h"
@@ -17,10 +22,27 @@ namespace qtt {
 namespace {
 constexpr int JT = 256;  // threads per CTA
 
-__device__ __forceinline__ double wsum(double v) {
+template <class T>
+__device__ __forceinline__ T wsum(T v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+
+template <class T>
+struct Eps;
+template <>
+struct Eps<double> {
+    // off-orthogonality accepted per column pair: p * eps64
+    __device__ static double tol(int p) { return 2.220446049250313e-16 * double(p); }
+};
+template <>
+struct Eps<float> {
+    // sqrt(p) * eps32: columns orthogonal to a few 1e-6 relative
+    __device__ static float tol(int p) { return 1.1920929e-07f * sqrtf(float(p)); }
+};
+
+__device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ float ldcg(const float *p) { return __ldcg(p); }
 
 // Round-robin (circle method) pairing of qp (even) players at round k in [0, qp-1):
 // slot 0 pairs player 0 with 1 + k; slot i > 0 pairs 1 + (k+i) mod (qp-1) with 1 + (k-i) mod (qp-1).
@@ -35,9 +57,65 @@ __device__ __forceinline__ void rr_pair(int qp, int k, int slot, int &a, int &b)
     }
 }
 
+template <class T>
+__global__ void k_pack(const double *__restrict__ src, T *__restrict__ work, const PackEntry *__restrict__ ents,
+                       const Chunk *__restrict__ chunks, const SectorDesc *__restrict__ secs) {
+    const Chunk ch = chunks[blockIdx.x];
+    const PackEntry e = ents[ch.seg];
+    const SectorDesc sd = secs[e.sector];
+    for (int i = threadIdx.x; i < ch.len; i += blockDim.x) {
+        int64_t k = ch.start + i;
+        int r = int(k / e.cols), c = int(k - int64_t(r) * e.cols);
+        int ar = e.r0 + r, ac = e.c0 + c;  // position in A (m x n)
+        int64_t w = sd.trans ? (int64_t(ac) + int64_t(ar) * sd.p) : (int64_t(ar) + int64_t(ac) * sd.p);
+        work[sd.w_off + w] = T(src[e.src_off + k]);
+    }
+}
+
+__device__ double block_sum_d(double v) {
+    __shared__ double red[32];
+    v = wsum(v);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+    if (w == 0) v = wsum(v);
+    return v;  // valid in thread 0
+}
+
+// eigh: symmetrise from one triangle, shift by the Frobenius norm (stored in the descriptor)
+template <class T>
+__global__ void k_eigh_prepare(T *work, SectorDesc *secs, int upper) {
+    SectorDesc &sd = secs[blockIdx.x];
+    const int n = sd.p;
+    T *W = work + sd.w_off;
+    for (int64_t t = threadIdx.x; t < int64_t(n) * n; t += blockDim.x) {
+        int i = int(t % n), j = int(t / n);
+        if (i == j) continue;
+        bool keep = upper ? (i < j) : (i > j);
+        if (!keep) continue;
+        W[j + int64_t(i) * n] = W[i + int64_t(j) * n];
+    }
+    __syncthreads();
+    double acc = 0.0;
+    for (int64_t t = threadIdx.x; t < int64_t(n) * n; t += blockDim.x) acc += double(W[t]) * double(W[t]);
+    acc = block_sum_d(acc);
+    __shared__ double shift;
+    if (threadIdx.x == 0) {
+        shift = sqrt(acc);
+        if (shift < 1.0e-200) shift = 1.0;
+        sd.shift = shift;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) W[i + int64_t(i) * n] += T(shift);
+}
+
+template <class T>
 struct JacobiParams {
-    double *work;
-    double *rot;
+    T *work;
+    T *rot;
     const SectorDesc *secs;
     const int *slot_start;  // nsec + 1 prefix sums of pairs per step
     int nsec;
@@ -50,12 +128,13 @@ struct JacobiParams {
 // One grid barrier per step.  Every CTA keeps its own copy of the per-sector
 // sweep / done state in shared memory and updates it identically after each
 // barrier from the rotation flags, so no second barrier is needed to publish it.
-__global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
+template <class T>
+__global__ void __launch_bounds__(JT) k_jacobi(JacobiParams<T> P) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ int jsh[];
     const int nsec = P.nsec;
-    int *done = jsh;            // nsec
-    int *sweep = jsh + nsec;    // nsec
+    int *done = jsh;          // nsec
+    int *sweep = jsh + nsec;  // nsec
     __shared__ int ndone;
     const int lane = threadIdx.x & 31;
     const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -64,11 +143,10 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
     const int64_t nt = int64_t(gridDim.x) * blockDim.x;
     const int total_slots = P.slot_start[nsec];
 
-    // rotation matrices start as identity; sectors with < 2 columns are done at once
     for (int s = 0; s < nsec; ++s) {
         const SectorDesc sd = P.secs[s];
         const int64_t qq = int64_t(sd.q) * sd.q;
-        for (int64_t e = gt; e < qq; e += nt) P.rot[sd.rot_off + e] = (e % (sd.q + 1) == 0) ? 1.0 : 0.0;
+        for (int64_t e = gt; e < qq; e += nt) P.rot[sd.rot_off + e] = (e % (sd.q + 1) == 0) ? T(1) : T(0);
     }
     if (threadIdx.x == 0) ndone = 0;
     __syncthreads();
@@ -82,7 +160,6 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
     for (int64_t step = 0; step < P.max_steps; ++step) {
         if (ndone >= nsec) break;
         for (int64_t slot = gw; slot < total_slots; slot += nw) {
-            // sector of this slot
             int lo = 0, hi = nsec - 1;
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
@@ -104,11 +181,11 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
                 a = b;
                 b = t;
             }
-            double *wa = P.work + sd.w_off + int64_t(a) * sd.p;
-            double *wb = P.work + sd.w_off + int64_t(b) * sd.p;
-            double al = 0.0, be = 0.0, ga = 0.0;
+            T *wa = P.work + sd.w_off + int64_t(a) * sd.p;
+            T *wb = P.work + sd.w_off + int64_t(b) * sd.p;
+            T al = 0, be = 0, ga = 0;
             for (int r = lane; r < sd.p; r += 32) {
-                double x = __ldcg(wa + r), y = __ldcg(wb + r);
+                T x = ldcg(wa + r), y = ldcg(wb + r);
                 al = fma(x, x, al);
                 be = fma(y, y, be);
                 ga = fma(x, y, ga);
@@ -116,32 +193,30 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
             al = wsum(al);
             be = wsum(be);
             ga = wsum(ga);
-            const double tol = 2.220446049250313e-16 * double(sd.p);
-            if (ga == 0.0 || fabs(ga) <= tol * sqrt(al) * sqrt(be)) continue;
-            const double zeta = (be - al) / (2.0 * ga);
-            double t;
-            if (fabs(zeta) > 1e150)
-                t = 0.5 / zeta;
+            if (ga == T(0) || fabs(ga) <= Eps<T>::tol(sd.p) * sqrt(al) * sqrt(be)) continue;
+            const T zeta = (be - al) / (T(2) * ga);
+            T t;
+            if (fabs(zeta) > T(1e18))
+                t = T(0.5) / zeta;
             else
-                t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-            const double c = 1.0 / sqrt(1.0 + t * t);
-            const double sn = c * t;
+                t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+            const T c = T(1) / sqrt(T(1) + t * t);
+            const T sn = c * t;
             for (int r = lane; r < sd.p; r += 32) {
-                double x = __ldcg(wa + r), y = __ldcg(wb + r);
+                T x = ldcg(wa + r), y = ldcg(wb + r);
                 wa[r] = c * x - sn * y;
                 wb[r] = sn * x + c * y;
             }
-            double *va = P.rot + sd.rot_off + int64_t(a) * sd.q;
-            double *vb = P.rot + sd.rot_off + int64_t(b) * sd.q;
+            T *va = P.rot + sd.rot_off + int64_t(a) * sd.q;
+            T *vb = P.rot + sd.rot_off + int64_t(b) * sd.q;
             for (int r = lane; r < sd.q; r += 32) {
-                double x = __ldcg(va + r), y = __ldcg(vb + r);
+                T x = ldcg(va + r), y = ldcg(vb + r);
                 va[r] = c * x - sn * y;
                 vb[r] = sn * x + c * y;
             }
             if (lane == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
         }
         grid.sync();
-        // end-of-sweep bookkeeping, identical in every CTA
         for (int s = threadIdx.x; s < nsec; s += blockDim.x) {
             if (done[s]) continue;
             const int q = P.secs[s].q;
@@ -163,25 +238,30 @@ __global__ void __launch_bounds__(JT) k_jacobi(JacobiParams P) {
 }
 
 // One CTA per sector: column norms, ordering, normalisation, completion.
-__global__ void __launch_bounds__(1024) k_finish(double *__restrict__ work, const double *__restrict__ rot,
+// scratch: at least p doubles per sector at offset w_off (the candidate vector).
+template <class T>
+__global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, const T *__restrict__ rot,
                                                  double *__restrict__ U, double *__restrict__ V,
-                                                 double *__restrict__ S, const SectorDesc *__restrict__ secs) {
+                                                 double *__restrict__ S, const SectorDesc *__restrict__ secs,
+                                                 double *__restrict__ scratch) {
     extern __shared__ double sh[];
     const SectorDesc sd = secs[blockIdx.x];
     const int q = sd.q, p = sd.p;
-    double *sig = sh;                                 // q values
-    int *perm = reinterpret_cast<int *>(sh + q);      // q ints
+    double *sig = sh;                             // q values
+    int *perm = reinterpret_cast<int *>(sh + q);  // q ints
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const double *W = work + sd.w_off;
-    const double *R = rot + sd.rot_off;
+    const T *W = work + sd.w_off;
+    const T *R = rot + sd.rot_off;
     for (int j = w; j < q; j += nwarp) {
         double acc = 0.0;
-        for (int r = lane; r < p; r += 32) acc = fma(W[int64_t(j) * p + r], W[int64_t(j) * p + r], acc);
+        for (int r = lane; r < p; r += 32) {
+            double x = double(W[int64_t(j) * p + r]);
+            acc = fma(x, x, acc);
+        }
         acc = wsum(acc);
         if (lane == 0) sig[j] = sqrt(acc);
     }
     __syncthreads();
-    // stable rank sort: svd descending by sigma, eigh ascending
     for (int j = threadIdx.x; j < q; j += blockDim.x) {
         double v = sig[j];
         int rk = 0;
@@ -194,12 +274,11 @@ __global__ void __launch_bounds__(1024) k_finish(double *__restrict__ work, cons
     }
     __syncthreads();
     if (sd.mode == 1) {
-        // eigh: eigenvalues sigma - shift, eigenvectors are the rotation columns
         const int n = q;
         for (int j = threadIdx.x; j < n; j += blockDim.x) S[sd.s_off + j] = sig[perm[j]] - sd.shift;
         for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
             int j = int(e / n), r = int(e % n);
-            U[sd.u_off + e] = R[int64_t(perm[j]) * n + r];
+            U[sd.u_off + e] = double(R[int64_t(perm[j]) * n + r]);
         }
         return;
     }
@@ -210,11 +289,11 @@ __global__ void __launch_bounds__(1024) k_finish(double *__restrict__ work, cons
     for (int64_t e = threadIdx.x; e < int64_t(q) * p; e += blockDim.x) {
         int j = int(e / p), r = int(e % p);
         double sj = sig[perm[j]];
-        Wside[e] = sj > 0.0 ? W[int64_t(perm[j]) * p + r] / sj : 0.0;
+        Wside[e] = sj > 0.0 ? double(W[int64_t(perm[j]) * p + r]) / sj : 0.0;
     }
     for (int64_t e = threadIdx.x; e < int64_t(q) * q; e += blockDim.x) {
         int j = int(e / q), r = int(e % q);
-        Rside[e] = R[int64_t(perm[j]) * q + r];
+        Rside[e] = double(R[int64_t(perm[j]) * q + r]);
     }
     __syncthreads();
     // complete null columns of the W side with unit vectors orthogonalised against
@@ -222,8 +301,7 @@ __global__ void __launch_bounds__(1024) k_finish(double *__restrict__ work, cons
     __shared__ double red[32];
     __shared__ double bcast;
     __shared__ int accepted;
-    // candidate vector: the sector's work columns are no longer read past this point
-    double *cand = work + sd.w_off;
+    double *cand = scratch + sd.w_off;
     for (int jz = 0; jz < q; ++jz) {
         if (sig[perm[jz]] > 0.0) continue;
         for (int e = 0; e < p; ++e) {
@@ -270,25 +348,25 @@ __global__ void __launch_bounds__(1024) k_finish(double *__restrict__ work, cons
         }
     }
 }
-}  // namespace
 
-void launch_jacobi(double *work, double *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags) {
-    if (nsec <= 0) return;
+template <class T>
+void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
+                 int max_sweeps, int *sweeps_out, int *flags) {
     static int nsm = 0;
-    if (!nsm) {
-        int dev = ctx().device;
-        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
-        cuda_check(cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
+    static bool attr = false;
+    if (!nsm) cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx().device), "SM count");
+    if (!attr) {
+        cuda_check(cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
                    "Jacobi smem attribute");
+        attr = true;
     }
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     int per_sm = 0;
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi, JT, smem), "occupancy");
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi<T>, JT, smem), "occupancy");
     per_sm = std::max(1, std::min(per_sm, 4));
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), ctx().stream), "memset flags");
-    JacobiParams P;
+    JacobiParams<T> P;
     P.work = work;
     P.rot = rot;
     P.secs = sec;
@@ -300,25 +378,69 @@ void launch_jacobi(double *work, double *rot, const SectorDesc *sec, const int *
     P.rotated = flags;
     void *args[] = {&P};
     dim3 grid(nsm * per_sm), block(JT);
-    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi, grid, block, args, smem, ctx().stream),
+    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi<T>, grid, block, args, smem, ctx().stream),
                "cooperative Jacobi launch");
     count_launch();
 }
 
-void launch_finish(double *work, const double *rot, double *U, double *V, double *s, const SectorDesc *sec,
-                   int nsec, int max_q) {
-    if (nsec <= 0) return;
+template <class T>
+void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
+                 int max_q, double *scratch) {
     size_t smem = size_t(max_q) * (sizeof(double) + sizeof(int)) + 16;
     static bool attr = false;
     if (!attr) {
-        cuda_check(cudaFuncSetAttribute(k_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+        cuda_check(cudaFuncSetAttribute(k_finish<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
                    "finish smem attribute");
         attr = true;
     }
     if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the SVD finishing kernel");
-    k_finish<<<nsec, 1024, smem, ctx().stream>>>(work, rot, U, V, s, sec);
+    k_finish<T><<<nsec, 1024, smem, ctx().stream>>>(work, rot, U, V, s, sec, scratch);
     count_launch();
     cuda_check(cudaGetLastError(), "SVD finishing kernel launch");
+}
+}  // namespace
+
+void launch_pack(const double *src, void *work, const PackEntry *e, const Chunk *chunks, int64_t nchunks,
+                 const SectorDesc *sec, int f32) {
+    if (nchunks <= 0) return;
+    if (f32)
+        k_pack<float><<<unsigned(nchunks), JT, 0, ctx().stream>>>(src, static_cast<float *>(work), e, chunks, sec);
+    else
+        k_pack<double><<<unsigned(nchunks), JT, 0, ctx().stream>>>(src, static_cast<double *>(work), e, chunks, sec);
+    count_launch();
+    cuda_check(cudaGetLastError(), "pack kernel launch");
+}
+
+void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f32) {
+    if (nsec <= 0) return;
+    if (f32)
+        k_eigh_prepare<float><<<nsec, JT, 0, ctx().stream>>>(static_cast<float *>(work), sec, upper);
+    else
+        k_eigh_prepare<double><<<nsec, JT, 0, ctx().stream>>>(static_cast<double *>(work), sec, upper);
+    count_launch();
+    cuda_check(cudaGetLastError(), "eigh prepare kernel launch");
+}
+
+void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32) {
+    if (nsec <= 0) return;
+    if (f32)
+        jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
+                    max_sweeps, sweeps_out, flags);
+    else
+        jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
+                    max_steps_per_sweep, max_sweeps, sweeps_out, flags);
+}
+
+void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
+                   int max_q, double *scratch, int f32) {
+    if (nsec <= 0) return;
+    if (f32)
+        finish_impl(static_cast<const float *>(work), static_cast<const float *>(rot), U, V, s, sec, nsec, max_q,
+                    scratch);
+    else
+        finish_impl(static_cast<const double *>(work), static_cast<const double *>(rot), U, V, s, sec, nsec, max_q,
+                    scratch);
 }
 
 }  // namespace qtt

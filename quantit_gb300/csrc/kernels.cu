@@ -128,46 +128,6 @@ __global__ void k_zero(double *p, int64_t n) {
         p[i] = 0.0;
 }
 
-// W is column-major p x q; W = A (m >= n) or A^T.
-__global__ void k_pack(const double *__restrict__ src, double *__restrict__ work, const PackEntry *__restrict__ ents,
-                       const Chunk *__restrict__ chunks, const SectorDesc *__restrict__ secs) {
-    const Chunk ch = chunks[blockIdx.x];
-    const PackEntry e = ents[ch.seg];
-    const SectorDesc sd = secs[e.sector];
-    for (int i = threadIdx.x; i < ch.len; i += blockDim.x) {
-        int64_t k = ch.start + i;
-        int r = int(k / e.cols), c = int(k - int64_t(r) * e.cols);
-        int ar = e.r0 + r, ac = e.c0 + c;  // position in A (m x n)
-        int64_t w = sd.trans ? (int64_t(ac) + int64_t(ar) * sd.p) : (int64_t(ar) + int64_t(ac) * sd.p);
-        work[sd.w_off + w] = src[e.src_off + k];
-    }
-}
-
-__global__ void k_eigh_prepare(double *work, SectorDesc *secs, int upper) {
-    SectorDesc &sd = secs[blockIdx.x];
-    const int n = sd.p;  // square
-    double *W = work + sd.w_off;
-    for (int64_t t = threadIdx.x; t < int64_t(n) * n; t += blockDim.x) {
-        int i = int(t % n), j = int(t / n);  // W(i, j) column-major
-        if (i == j) continue;
-        bool keep = upper ? (i < j) : (i > j);
-        if (!keep) continue;
-        W[j + int64_t(i) * n] = W[i + int64_t(j) * n];  // mirror into the other triangle
-    }
-    __syncthreads();
-    double acc = 0.0;
-    for (int64_t t = threadIdx.x; t < int64_t(n) * n; t += blockDim.x) acc = fma(W[t], W[t], acc);
-    acc = block_sum(acc);
-    __shared__ double shift;
-    if (threadIdx.x == 0) {
-        shift = sqrt(acc) + 1.0e-300;
-        if (shift < 1.0e-200) shift = 1.0;
-        sd.shift = shift;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) W[i + int64_t(i) * n] += shift;
-}
-
 __global__ void k_scatter(const double *__restrict__ src, double *__restrict__ dst,
                           const ScatterEntry *__restrict__ ents, const Chunk *__restrict__ chunks) {
     const Chunk ch = chunks[blockIdx.x];
@@ -264,21 +224,6 @@ void launch_zero(double *p, int64_t n) {
     k_zero<<<unsigned(g), TPB, 0, ctx().stream>>>(p, n);
     count_launch();
     cuda_check(cudaGetLastError(), "zero kernel launch");
-}
-
-void launch_pack(const double *src, double *work, const PackEntry *e, const Chunk *chunks, int64_t nchunks,
-                 const SectorDesc *sec) {
-    if (nchunks <= 0) return;
-    k_pack<<<grid_for(nchunks), TPB, 0, ctx().stream>>>(src, work, e, chunks, sec);
-    count_launch();
-    cuda_check(cudaGetLastError(), "pack kernel launch");
-}
-
-void launch_eigh_prepare(double *work, SectorDesc *sec, int nsec, int upper) {
-    if (nsec <= 0) return;
-    k_eigh_prepare<<<nsec, TPB, 0, ctx().stream>>>(work, sec, upper);
-    count_launch();
-    cuda_check(cudaGetLastError(), "eigh prepare kernel launch");
 }
 
 void launch_scatter(const double *src, double *dst, const ScatterEntry *e, const Chunk *chunks, int64_t nchunks) {

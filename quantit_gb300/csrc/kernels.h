@@ -118,24 +118,25 @@ struct PackEntry {
     int32_t sector, rows, cols, r0, c0, pad;
 };
 void launch_zero(double *p, int64_t n);
-void launch_pack(const double *src, double *work, const PackEntry *e, const Chunk *chunks, int64_t nchunks,
-                 const SectorDesc *sec);
+// The work / rotation buffers hold float when f32 != 0 (mixed path), else double.
+void launch_pack(const double *src, void *work, const PackEntry *e, const Chunk *chunks, int64_t nchunks,
+                 const SectorDesc *sec, int f32);
 // eigh: symmetrise W from one triangle, then shift the diagonal by the sector's
 // Frobenius norm (written back into sec[s].shift) so the matrix is positive definite.
-void launch_eigh_prepare(double *work, SectorDesc *sec, int nsec, int upper);
+void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f32);
 // Batched one-sided Jacobi over all sectors in one cooperative launch.
 // slot_start[nsec+1]: prefix sums of the pairs each sector contributes per step
 // ((q + q%2)/2); max_steps_per_sweep = max over sectors of (q + q%2 - 1).
 // sweeps_out[s] receives the number of sweeps sector s used; flags holds
-// 2*nsec+1 ints of scratch.
-void launch_jacobi(double *work, double *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags);
+// nsec*max_sweeps ints of scratch.
+void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32);
 // Column norms, sort (descending for svd, ascending eigenvalues for eigh),
 // normalisation and completion of null columns; writes U (m x k), V (n x k)
-// column-major and s (k) per sector, k = min(m, n).
-// The work buffer is reused as scratch.  max_q: largest q over the sectors.
-void launch_finish(double *work, const double *rot, double *U, double *V, double *s, const SectorDesc *sec,
-                   int nsec, int max_q);
+// column-major and s (k) per sector in FP64, k = min(m, n).  max_q: largest q;
+// scratch: FP64 buffer with the work buffer's element offsets.
+void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec,
+                   int nsec, int max_q, double *scratch, int f32);
 // Segment = one output block (rows x k row-major at dst_off) from a column-major
 // (ld x *) sector matrix at src_off: dst[i*k + j] = src[src_off + (r0 + i) + j*ld].
 struct ScatterEntry {

@@ -193,14 +193,17 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     }
     D.total_k = stot;
     const int nsec = int(D.desc.size());
-    D.work = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
-    D.rot = dev_alloc(size_t(std::max<int64_t>(rtot, 1)) * 8);
+    // the mixed path (split-precision block GEMMs) also runs its sector SVDs in FP32
+    const int f32 = gemm_mode() != GEMM_F64 ? 1 : 0;
+    const size_t es = f32 ? 4 : 8;
+    D.work = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * es);
+    D.rot = dev_alloc(size_t(std::max<int64_t>(rtot, 1)) * es);
     D.U = dev_alloc(size_t(std::max<int64_t>(utot, 1)) * 8);
     D.V = dev_alloc(size_t(std::max<int64_t>(vtot, 1)) * 8);
     D.S = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * 8);
     if (nsec == 0) return;
-    double *W = static_cast<double *>(D.work->p);
-    launch_zero(W, wtot);
+    void *W = D.work->p;
+    cuda_check(cudaMemsetAsync(W, 0, size_t(wtot) * es, ctx().stream), "cudaMemsetAsync(work)");
     // pack entries: one per (block, batch element)
     std::vector<PackEntry> pe;
     std::vector<int64_t> lens;
@@ -230,9 +233,9 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     {
         StatScope sc(ST_PACK, 2.0 * 8.0 * double(std::accumulate(lens.begin(), lens.end(), int64_t(0))));
         launch_pack(static_cast<const double *>(t.data()), W, upload_vec(pe), upload_vec(chunks),
-                    int64_t(chunks.size()), dsec);
+                    int64_t(chunks.size()), dsec, f32);
     }
-    if (mode == 1) launch_eigh_prepare(W, dsec, nsec, upper);
+    if (mode == 1) launch_eigh_prepare(W, dsec, nsec, upper, f32);
     const int max_sweeps = 80;
     auto ibuf = dev_alloc(size_t(nsec) * (max_sweeps + 1) * sizeof(int));
     int *sweeps = static_cast<int *>(ibuf->p);
@@ -240,12 +243,12 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     last_sweeps() = {ibuf, nsec};
     double est = 0;
     for (auto &d : D.desc) est += 8.0 * double(d.q) * double(d.q) * (6.0 * d.p + 4.0 * d.q);
+    BufPtr scratch = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
     {
         StatScope sc(ST_SVD, est);
-        launch_jacobi(W, static_cast<double *>(D.rot->p), dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps,
-                      flags);
-        launch_finish(W, static_cast<double *>(D.rot->p), static_cast<double *>(D.U->p),
-                      static_cast<double *>(D.V->p), static_cast<double *>(D.S->p), dsec, nsec, max_q);
+        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32);
+        launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
+                      static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32);
     }
 }
 

@@ -77,13 +77,22 @@ def test_tc_gemm_tensorgdot_epilogue(tf32x3):
 
 
 def test_mixed_dmrg_energy_close_to_fp64():
-    L, D = 12, 32
-    mpo = o.heisenberg_mpo(L)
-    mps = o.right_canonicalize(o.random_mps(L, D, [1, -1], 0, np.random.default_rng(5)))
-    dmpo = q.networks.bMPO([to_device(t) for t in mpo])
-    res = {}
-    for mode in ("f64", "tf32x3"):
-        dmps = q.networks.bMPS([to_device(t) for t in mps], 0)
-        res[mode] = q.algorithms.dmrg(dmpo, dmps, q.algorithms.dmrg_options(
-            cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4, maximum_iterations=4, gemm=mode))
-    assert abs(res["tf32x3"] - res["f64"]) / L < 1e-8, res
+    """Converged runs: the mixed path (split-TF32 block GEMMs, FP32 sector SVD)
+    reports the FP64 variational energy of its final state, which matches the
+    plain FP64 path to better than 1e-8 per site.  (Its per-bond Ritz values carry
+    ~1e-6 relative noise from FP32 accumulation and are not used for the result.)"""
+    for L, D, sweeps in ((10, 64, 10), (16, 64, 12)):
+        mpo = o.heisenberg_mpo(L)
+        mps = o.right_canonicalize(o.random_mps(L, D, [1, -1], 0, np.random.default_rng(5)))
+        dmpo = q.networks.bMPO([to_device(t) for t in mpo])
+        res = {}
+        for mode in ("f64", "tf32x3"):
+            dmps = q.networks.bMPS([to_device(t) for t in mps], 0)
+            res[mode] = q.algorithms.dmrg(dmpo, dmps, q.algorithms.dmrg_options(
+                cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4, maximum_iterations=sweeps,
+                gemm=mode))
+            e, n2 = q.algorithms.mps_energy(dmpo, dmps)
+            assert abs(n2 - 1.0) < 1e-5
+            if mode == "tf32x3":
+                assert res[mode] == pytest.approx(e / n2, rel=1e-14)
+        assert abs(res["tf32x3"] - res["f64"]) / L < 1e-8, (L, D, res)
