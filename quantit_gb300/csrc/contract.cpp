@@ -115,6 +115,7 @@ ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_
     p2.insert(p2.end(), P.freeB.begin(), P.freeB.end());
     p2p.insert(p2p.end(), P.dB.begin(), P.dB.end());
     P.p1 = p1;
+    P.p2p = p2p;
     P.p2 = p2;
     // output structure (compute_tdot_cval_sectSize :1908-1935)
     BT &o = P.out;
@@ -231,34 +232,92 @@ int64_t prod_sizes(const BT &t, int64_t b, const std::vector<int64_t> &dims) {
 }
 }  // namespace
 
+namespace {
+// Split every block of t (legs permuted by perm; the first nrow legs form the
+// rows, the rest the contracted K) into hi / lo TF32 arrays in matrix form.
+void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std::vector<int64_t> &offs, BufPtr &hi,
+                   BufPtr &lo) {
+    const int r = t.rank;
+    const int64_t nb = t.nblocks();
+    offs.assign(nb, 0);
+    std::vector<SplitEntry> ents(nb);
+    std::vector<int64_t> lens(nb);
+    int64_t o = 0;
+    for (int64_t b = 0; b < nb; ++b) {
+        int64_t shp[MAXRANK], str[MAXRANK];
+        t.block_shape(b, shp);
+        int64_t s = 1;
+        for (int d = r - 1; d >= 0; --d) {
+            str[d] = s;
+            s *= shp[d];
+        }
+        SplitEntry &e = ents[b];
+        std::memset(&e, 0, sizeof(e));
+        int64_t rows = 1, K = 1;
+        for (int i = 0; i < r; ++i) {
+            e.dims[i] = shp[perm[i]];
+            e.stride[i] = str[perm[i]];
+            (i < nrow ? rows : K) *= shp[perm[i]];
+        }
+        if (K > INT32_MAX) fail(ERR_INVALID_ARGUMENT, "contracted dimension too large");
+        const int64_t K4 = (K + 3) & ~int64_t(3);
+        e.src_off = t.boff[b];
+        e.dst_off = o;
+        e.rank = r;
+        e.K = int32_t(K);
+        e.K4 = int32_t(K4);
+        offs[b] = o;
+        lens[b] = rows * K;
+        o += rows * K4;
+    }
+    const size_t bytes = size_t(std::max<int64_t>(o, 4)) * sizeof(float);
+    hi = dev_alloc(bytes);
+    lo = dev_alloc(bytes);
+    cuda_check(cudaMemsetAsync(hi->p, 0, bytes, ctx().stream), "cudaMemsetAsync(split)");
+    cuda_check(cudaMemsetAsync(lo->p, 0, bytes, ctx().stream), "cudaMemsetAsync(split)");
+    auto chunks = make_chunks(lens);
+    StatScope sc(ST_PACK, 16.0 * double(std::accumulate(lens.begin(), lens.end(), int64_t(0))));
+    launch_split_tf32(static_cast<const double *>(t.data()), static_cast<float *>(hi->p), static_cast<float *>(lo->p),
+                      upload_vec(ents), upload_vec(chunks), int64_t(chunks.size()));
+}
+}  // namespace
+
 void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, const BT *add, double beta,
                      double alpha, const std::vector<int64_t> *add_block) {
     require_f64(A);
     require_f64(B);
     const int64_t nout = int64_t(P.out_p0.size());
     if (nout == 0) return;
+    const int mode = gemm_mode();
+    const bool tc = mode != GEMM_F64;
     // operand buffers
-    BufPtr pa, pb;
+    BufPtr pa, pb, ahi, alo, bhi, blo;
     std::vector<int64_t> offa, offb;
     const double *Ap = static_cast<const double *>(A.data());
     const double *Bp = static_cast<const double *>(B.data());
     const std::vector<int64_t> *oa = &A.boff, *ob = &B.boff;
     int a_t = 0, b_t = 0;
-    if (P.a_mode == 1) a_t = 1;
-    if (P.a_mode == 2) {
-        pa = pack_operand(A, P.p1, offa);
-        Ap = static_cast<const double *>(pa->p);
+    if (tc) {
+        split_operand(A, P.p1, int(P.freeA.size()), offa, ahi, alo);
+        split_operand(B, P.p2p, int(P.freeB.size()), offb, bhi, blo);
         oa = &offa;
-    }
-    if (P.b_mode == 1) b_t = 1;
-    if (P.b_mode == 2) {
-        pb = pack_operand(B, P.p2, offb);
-        Bp = static_cast<const double *>(pb->p);
         ob = &offb;
+    } else {
+        if (P.a_mode == 1) a_t = 1;
+        if (P.a_mode == 2) {
+            pa = pack_operand(A, P.p1, offa);
+            Ap = static_cast<const double *>(pa->p);
+            oa = &offa;
+        }
+        if (P.b_mode == 1) b_t = 1;
+        if (P.b_mode == 2) {
+            pb = pack_operand(B, P.p2, offb);
+            Bp = static_cast<const double *>(pb->p);
+            ob = &offb;
+        }
     }
-    const int mode = gemm_mode();
-    const int TM = mode == GEMM_F64 ? 64 : gemm_tile_m(mode);
-    const int TN = mode == GEMM_F64 ? 64 : gemm_tile_n(mode);
+    const int TM = tc ? gemm_tile_m(mode) : 64;
+    const int TN = tc ? gemm_tile_n(mode) : 64;
     std::vector<GemmPair> pairs(P.pair_a.size());
     std::vector<GemmOut> outs(nout);
     std::vector<GemmTile> tiles;
@@ -292,24 +351,42 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
     std::stable_sort(wt.begin(), wt.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
     tiles.reserve(wt.size());
     for (auto &w : wt) tiles.push_back(w.second);
-    GemmArgs g;
-    g.A = Ap;
-    g.B = Bp;
-    g.C = static_cast<double *>(out.data());
-    g.Cadd = add ? static_cast<const double *>(add->data()) : nullptr;
-    g.pairs = upload_vec(pairs);
-    g.outs = upload_vec(outs);
-    g.tiles = upload_vec(tiles);
-    g.ntiles = int32_t(tiles.size());
-    g.a_t = a_t;
-    g.b_t = b_t;
-    g.alpha = alpha;
-    g.beta = beta;
+    const GemmPair *dpairs = upload_vec(pairs);
+    const GemmOut *douts = upload_vec(outs);
+    const GemmTile *dtiles = upload_vec(tiles);
     StatScope sc(ST_GEMM, flops);
-    if (mode == GEMM_F64)
+    if (!tc) {
+        GemmArgs g;
+        g.A = Ap;
+        g.B = Bp;
+        g.C = static_cast<double *>(out.data());
+        g.Cadd = add ? static_cast<const double *>(add->data()) : nullptr;
+        g.pairs = dpairs;
+        g.outs = douts;
+        g.tiles = dtiles;
+        g.ntiles = int32_t(tiles.size());
+        g.a_t = a_t;
+        g.b_t = b_t;
+        g.alpha = alpha;
+        g.beta = beta;
         launch_gemm_f64(g);
-    else
+    } else {
+        TcArgs g;
+        g.Ahi = static_cast<const float *>(ahi->p);
+        g.Alo = static_cast<const float *>(alo->p);
+        g.Bhi = static_cast<const float *>(bhi->p);
+        g.Blo = static_cast<const float *>(blo->p);
+        g.C = static_cast<double *>(out.data());
+        g.Cadd = add ? static_cast<const double *>(add->data()) : nullptr;
+        g.pairs = dpairs;
+        g.outs = douts;
+        g.tiles = dtiles;
+        g.ntiles = int32_t(tiles.size());
+        g.pad = 0;
+        g.alpha = alpha;
+        g.beta = beta;
         launch_gemm_tc(g, mode);
+    }
 }
 
 BT tensordot(const BT &a, const BT &b, const std::vector<int64_t> &da, const std::vector<int64_t> &db) {

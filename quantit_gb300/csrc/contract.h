@@ -11,6 +11,7 @@ namespace qtt {
 // accumulation order, and how each operand is read.
 struct ContractPlan {
     std::vector<int64_t> dA, dB, freeA, freeB, p1, p2;
+    std::vector<int64_t> p2p;  // B legs as (free, contracted): B blocks in (N x K) matrix form
     BT out;                               // structure and compact offsets
     std::vector<int64_t> pair_a, pair_b;  // source blocks of each matched pair
     std::vector<int64_t> out_p0, out_p1;  // pair range of each output block

@@ -1,20 +1,25 @@
 // Grouped block GEMM on the 5th-generation tensor cores (tcgen05) with
 // split-precision TF32 operands: every FP64 operand element x is split into
 // hi = tf32(x) and lo = tf32(x - hi), and each output tile accumulates
-//     A_hi B_hi + A_hi B_lo + A_lo B_hi
+//     A_hi B_lo + A_lo B_hi + A_hi B_hi
 // in FP32 in tensor memory (TMEM).  The dropped A_lo B_lo term and the FP32
 // accumulation leave about FP32 accuracy (~1e-7 relative) at a third of the TF32
 // tensor throughput -- the "compensated (split-precision) products" of the mixed
 // path; everything outside the block GEMMs stays FP64.
 //
-// CTA = one 128 x 128 tile of one output block (same tile/pair tables as the FP64
-// kernel).  All 8 warps produce: they read FP64 A / B from global memory (plain,
-// transposed or packed layouts), split, and store hi/lo into a 2-stage shared
-// memory ring in the canonical no-swizzle K-major UMMA layout (core matrices of
-// 8 rows x 16 bytes).  Thread 0 issues the tcgen05.mma instructions of a stage
-// (3 products x 4 k-steps of 8) and commits them to that stage's mbarrier, which
-// the producers wait on before refilling the stage.  The epilogue reads the
-// accumulator with tcgen05.ld and writes alpha*acc + beta*add in FP64.
+// Two kernels:
+//  * k_split_tf32: one pass over the operand blocks writes hi / lo as FP32 bit
+//    patterns in matrix form (rows x K4, K contiguous, zero padded to a multiple
+//    of 4).  The FP64 -> FP32 conversion uses integer operations only: GB300's FP64
+//    pipe is a small fraction of its FP32 / integer rate.
+//  * k_gemm_tf32x3: CTA = one 128 x 128 tile of one output block (same tile and
+//    pair tables as the FP64 kernel).  All 8 warps copy 16-byte vectors of the
+//    split operands into a 2-stage shared-memory ring in the canonical no-swizzle
+//    K-major UMMA layout (core matrices of 8 rows x 16 bytes).  Thread 0 issues
+//    the tcgen05.mma instructions of a stage (3 products x 4 k-steps of 8) and
+//    commits them to that stage's mbarrier, which the producers wait on before
+//    refilling the stage.  The epilogue reads the accumulator with tcgen05.ld and
+//    writes alpha*acc + beta*add in FP64.
 //
 // Every mbarrier wait is bounded; on timeout the kernel records an error code in
 // a device word that the host checks, still waits (bounded) for its MMAs and
@@ -30,13 +35,12 @@ namespace {
 constexpr int TBM = 128, TBN = 128, TBK = 32;  // tile and K chunk (elements)
 constexpr int TTHREADS = 256;
 constexpr int TMEM_COLS = 128;  // FP32 accumulator columns (N)
-// one operand copy (rows x TBK tf32) = rows * 128 bytes; core matrix = 8 rows x 16 B
-constexpr int A_BYTES = TBM * TBK * 4;  // 16 KB
+constexpr int A_BYTES = TBM * TBK * 4;  // one operand copy: 16 KB
 constexpr int B_BYTES = TBN * TBK * 4;  // 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi/lo of A and B: 64 KB
 constexpr int NSTAGE = 2;
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024;
-constexpr uint32_t LBO = 128;               // K-adjacent core matrices
+constexpr uint32_t LBO = 128;                   // K-adjacent core matrices
 constexpr uint32_t SBO = (TBK * 4 / 16) * 128;  // next 8-row group: 1024 B
 constexpr long long WAIT_LIMIT = 1ll << 22;
 
@@ -50,8 +54,7 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
     d |= uint64_t(LBO >> 4) << 16;
     d |= uint64_t(SBO >> 4) << 32;
     d |= uint64_t(1) << 46;  // descriptor version for tcgen05
-    // base offset 0, no swizzle (layout type 0)
-    return d;
+    return d;                // base offset 0, no swizzle (layout type 0)
 }
 
 // kind::tf32, D=F32, A=B=TF32, both K-major, N=128, M=128
@@ -83,22 +86,98 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
     return r;
 }
 
-// byte offset of element (row r, k) in one operand copy
+// FP64 -> FP32 (round to nearest, ties away) with integer operations only.
+// Magnitudes below the FP32 normal range flush to zero.
+__device__ __forceinline__ float f64_to_f32_int(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const uint32_t sign = uint32_t(b >> 63) << 31;
+    const int e = int((b >> 52) & 0x7FF);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    uint32_t f;
+    if (e == 0) {
+        f = 0;
+    } else if (e == 0x7FF) {
+        f = 0x7F800000u | (m ? 0x400000u : 0u);
+    } else {
+        const int fe = e - 1023 + 127;
+        if (fe <= 0) {
+            f = 0;
+        } else if (fe >= 255) {
+            f = 0x7F800000u;
+        } else {
+            const unsigned long long em = ((unsigned long long)fe << 52 | m) + (1ull << 28);
+            f = uint32_t(em >> 29);
+            if (f >= 0x7F800000u) f = 0x7F800000u;
+        }
+    }
+    return __uint_as_float(sign | f);
+}
+
+__global__ void k_split_tf32(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo,
+                             const SplitEntry *__restrict__ ents, const Chunk *__restrict__ chunks) {
+    const Chunk ch = chunks[blockIdx.x];
+    const SplitEntry &e = ents[ch.seg];
+    const int r = e.rank;
+    for (int i = threadIdx.x; i < ch.len; i += blockDim.x) {
+        const int64_t lin = ch.start + i;
+        int64_t rem = lin, so = e.src_off;
+        for (int d = r - 1; d >= 0; --d) {
+            const int64_t n = e.dims[d];
+            const int64_t q = rem / n;
+            so += (rem - q * n) * e.stride[d];
+            rem = q;
+        }
+        const float xf = f64_to_f32_int(src[so]);
+        const uint32_t h = to_tf32(xf);
+        const uint32_t l = to_tf32(xf - __uint_as_float(h));
+        const int64_t row = lin / e.K, k = lin - row * e.K;
+        const int64_t dst = e.dst_off + row * e.K4 + k;
+        hi[dst] = __uint_as_float(h);
+        lo[dst] = __uint_as_float(l);
+    }
+}
+
+// byte offset of (row r, k) in one operand copy of the canonical K-major layout
 __device__ __forceinline__ uint32_t kmaj_off(int r, int k) {
     return uint32_t(r >> 3) * SBO + uint32_t(k >> 2) * LBO + uint32_t(r & 7) * 16u + uint32_t(k & 3) * 4u;
 }
 
-__device__ __forceinline__ void split_store(char *hi, char *lo, uint32_t off, double x) {
-    const uint32_t h = to_tf32(float(x));
-    const double rem = x - double(__uint_as_float(h));
-    const uint32_t l = to_tf32(float(rem));
-    *reinterpret_cast<uint32_t *>(hi + off) = h;
-    *reinterpret_cast<uint32_t *>(lo + off) = l;
+__device__ __forceinline__ void st_shared_v4(char *p, uint4 v) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(smem_u32(p)), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w)
+                 : "memory");
 }
 
-__global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(GemmArgs g, int *err) {
+// rows x (TBK / 4) 16-byte vectors of one operand tile (hi and lo) into shared memory
+template <int ROWS>
+__device__ __forceinline__ void load_tile(const float *__restrict__ hi, const float *__restrict__ lo, int64_t off,
+                                          int rows_valid, int row0, int K4, int k0, char *shi, char *slo, int tid) {
+#pragma unroll
+    for (int i = 0; i < (ROWS * (TBK / 4)) / TTHREADS; ++i) {
+        const int e = tid + i * TTHREADS;
+        const int row = e >> 3, kc = e & 7;
+        const int gr = row0 + row, gk = k0 + kc * 4;
+        uint4 vh = make_uint4(0, 0, 0, 0), vl = make_uint4(0, 0, 0, 0);
+        if (gr < rows_valid && gk < K4) {
+            const int64_t idx = off + int64_t(gr) * K4 + gk;
+            vh = __ldg(reinterpret_cast<const uint4 *>(hi + idx));
+            vl = __ldg(reinterpret_cast<const uint4 *>(lo + idx));
+        }
+        const uint32_t so = kmaj_off(row, kc * 4);
+        st_shared_v4(shi + so, vh);
+        st_shared_v4(slo + so, vl);
+    }
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n}\n" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err) {
     extern __shared__ __align__(1024) char smem_raw[];
-    // align the ring to 1024 bytes
     char *smem = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     __shared__ uint64_t mbar[NSTAGE];
     __shared__ uint32_t tmem_base_sh;
@@ -123,15 +202,13 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(GemmArgs g, int *er
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base_sh;
 
-    // chunk list of this output block: (pair, k0) in pair order
     int nchunk = 0;
-    for (int p = o.p0; p < o.p1; ++p) nchunk += (g.pairs[p].K + TBK - 1) / TBK;
+    for (int p = o.p0; p < o.p1; ++p) nchunk += ((g.pairs[p].K + 3) / 4 * 4 + TBK - 1) / TBK;
 
     int p = o.p0, k0 = 0;
     uint32_t commits[NSTAGE] = {0, 0};
     for (int c = 0; c < nchunk; ++c) {
         const int s = c % NSTAGE;
-        // wait until the MMAs that last read this stage are complete
         if (c >= NSTAGE) {
             if (!mbar_wait(&mbar[s], (commits[s] - 1) & 1)) {
                 if (tid == 0) atomicExch(err, 1);
@@ -140,51 +217,16 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(GemmArgs g, int *er
         }
         __syncthreads();
         if (abort_flag) break;
-        // advance to the chunk's pair
-        while (k0 >= g.pairs[p].K) {
+        while (k0 >= ((g.pairs[p].K + 3) & ~3)) {
             ++p;
             k0 = 0;
         }
         const GemmPair pr = g.pairs[p];
-        const int K = pr.K;
-        const double *__restrict__ A = g.A + pr.a_off;
-        const double *__restrict__ B = g.B + pr.b_off;
+        const int K4 = (pr.K + 3) & ~3;
         char *st = smem + s * STAGE_BYTES;
         char *ahi = st, *alo = st + A_BYTES, *bhi = st + 2 * A_BYTES, *blo = st + 2 * A_BYTES + B_BYTES;
-        // A tile: 128 rows (m) x 32 (k)
-#pragma unroll 4
-        for (int i = 0; i < (TBM * TBK) / TTHREADS; ++i) {
-            const int e = tid + i * TTHREADS;
-            int m, k;
-            if (!g.a_t) {
-                k = e & (TBK - 1);
-                m = e / TBK;
-            } else {
-                m = e & (TBM - 1);
-                k = e / TBM;
-            }
-            const int gm = t.m0 + m, gk = k0 + k;
-            double x = 0.0;
-            if (gm < o.M && gk < K) x = g.a_t ? A[int64_t(gk) * o.M + gm] : A[int64_t(gm) * K + gk];
-            split_store(ahi, alo, kmaj_off(m, k), x);
-        }
-        // B tile stored N-rows x K (K-major): 128 (n) x 32 (k)
-#pragma unroll 4
-        for (int i = 0; i < (TBN * TBK) / TTHREADS; ++i) {
-            const int e = tid + i * TTHREADS;
-            int n, k;
-            if (!g.b_t) {
-                n = e & (TBN - 1);
-                k = e / TBN;
-            } else {
-                k = e & (TBK - 1);
-                n = e / TBK;
-            }
-            const int gn = t.n0 + n, gk = k0 + k;
-            double x = 0.0;
-            if (gn < o.N && gk < K) x = g.b_t ? B[int64_t(gn) * K + gk] : B[int64_t(gk) * o.N + gn];
-            split_store(bhi, blo, kmaj_off(n, k), x);
-        }
+        load_tile<TBM>(g.Ahi, g.Alo, pr.a_off, o.M, t.m0, K4, k0, ahi, alo, tid);
+        load_tile<TBN>(g.Bhi, g.Blo, pr.b_off, o.N, t.n0, K4, k0, bhi, blo, tid);
         k0 += TBK;
         // make the generic-proxy stores visible to the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -196,22 +238,11 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(GemmArgs g, int *er
 #pragma unroll
             for (int ks = 0; ks < TBK / 8; ++ks) {
                 const uint32_t koff = uint32_t(ks) * 2u * LBO;  // 8 tf32 = 2 core matrices along K
-                const uint64_t dAh = make_desc(a_hi + koff), dAl = make_desc(a_lo + koff);
-                const uint64_t dBh = make_desc(b_hi + koff), dBl = make_desc(b_lo + koff);
-                // small terms first, then the leading product
                 const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
-                asm volatile(
-                    "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n}\n" ::"r"(tmem),
-                    "l"(dAh), "l"(dBl), "r"(idesc), "r"(acc0));
-                asm volatile(
-                    "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n}\n" ::"r"(tmem),
-                    "l"(dAl), "l"(dBh), "r"(idesc), "r"(1u));
-                asm volatile(
-                    "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n}\n" ::"r"(tmem),
-                    "l"(dAh), "l"(dBh), "r"(idesc), "r"(1u));
+                // small terms first, then the leading product
+                mma_tf32(tmem, make_desc(a_hi + koff), make_desc(b_lo + koff), idesc, acc0);
+                mma_tf32(tmem, make_desc(a_lo + koff), make_desc(b_hi + koff), idesc, 1u);
+                mma_tf32(tmem, make_desc(a_hi + koff), make_desc(b_hi + koff), idesc, 1u);
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                              smem_u32(&mbar[s]))
@@ -219,7 +250,6 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(GemmArgs g, int *er
         }
         commits[s] += 1;
     }
-    // wait for every outstanding commit before reading the accumulator (or freeing TMEM)
     for (int s = 0; s < NSTAGE; ++s) {
         if (commits[s] == 0) continue;
         if (!mbar_wait(&mbar[s], (commits[s] - 1) & 1)) {
@@ -291,7 +321,15 @@ int *err_word() {
 int gemm_tile_m(int) { return TBM; }
 int gemm_tile_n(int) { return TBN; }
 
-void launch_gemm_tc(const GemmArgs &a, int mode) {
+void launch_split_tf32(const double *src, float *hi, float *lo, const SplitEntry *e, const Chunk *chunks,
+                       int64_t nchunks) {
+    if (nchunks <= 0) return;
+    k_split_tf32<<<unsigned(nchunks), 256, 0, ctx().stream>>>(src, hi, lo, e, chunks);
+    count_launch();
+    cuda_check(cudaGetLastError(), "split kernel launch");
+}
+
+void launch_gemm_tc(const TcArgs &a, int mode) {
     if (mode != GEMM_TF32X3) fail(ERR_INVALID_ARGUMENT, "this tensor-core GEMM precision mode is not built");
     if (a.ntiles <= 0) return;
     static bool attr = false;

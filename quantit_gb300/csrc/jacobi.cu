@@ -20,7 +20,8 @@ namespace cg = cooperative_groups;
 
 namespace qtt {
 namespace {
-constexpr int JT = 256;  // threads per CTA
+constexpr int JT = 256;   // threads per CTA of the packing kernels
+constexpr int JJ = 1024;  // threads per CTA of the Jacobi kernel: one CTA per SM keeps the grid barrier cheap
 
 template <class T>
 __device__ __forceinline__ T wsum(T v) {
@@ -129,7 +130,7 @@ struct JacobiParams {
 // sweep / done state in shared memory and updates it identically after each
 // barrier from the rotation flags, so no second barrier is needed to publish it.
 template <class T>
-__global__ void __launch_bounds__(JT) k_jacobi(JacobiParams<T> P) {
+__global__ void __launch_bounds__(JJ, 1) k_jacobi(JacobiParams<T> P) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ int jsh[];
     const int nsec = P.nsec;
@@ -363,8 +364,9 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     int per_sm = 0;
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi<T>, JT, smem), "occupancy");
-    per_sm = std::max(1, std::min(per_sm, 4));
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi<T>, JJ, smem), "occupancy");
+    if (per_sm < 1) fail(ERR_RUNTIME, "the Jacobi kernel cannot be resident on an SM");
+    per_sm = 1;
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), ctx().stream), "memset flags");
     JacobiParams<T> P;
     P.work = work;
@@ -377,7 +379,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     P.sweeps = sweeps_out;
     P.rotated = flags;
     void *args[] = {&P};
-    dim3 grid(nsm * per_sm), block(JT);
+    dim3 grid(nsm * per_sm), block(JJ);
     cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi<T>, grid, block, args, smem, ctx().stream),
                "cooperative Jacobi launch");
     count_launch();

@@ -61,8 +61,33 @@ struct GemmArgs {
     double alpha, beta;
 };
 void launch_gemm_f64(const GemmArgs &a);
-// Split-precision tensor-core variant (tcgen05); mode as GemmMode.
-void launch_gemm_tc(const GemmArgs &a, int mode);
+
+// Split-precision tensor-core variant (tcgen05).  Operands are first converted,
+// block by block, into "matrix form" split arrays: hi = tf32(x), lo = tf32(x - hi)
+// as FP32 bit patterns, rows x K4 row-major (K contiguous, K4 = K rounded up to 4,
+// zero padded), so the GEMM producers only move 16-byte vectors.
+// Segment = one operand block; element e of the (rows x K) matrix reads
+// src[src_off + sum_d idx_d(e) * stride[d]] with idx(e) the row-major index over dims.
+struct SplitEntry {
+    int64_t src_off, dst_off;  // dst_off: element offset into hi / lo, multiple of 4
+    int32_t rank, K, K4, pad;
+    int64_t dims[8];
+    int64_t stride[8];
+};
+void launch_split_tf32(const double *src, float *hi, float *lo, const SplitEntry *e, const Chunk *chunks,
+                       int64_t nchunks);
+// A pair's a_off / b_off index the split arrays; A rows = M, B rows = N, K4 = (K + 3) & ~3.
+struct TcArgs {
+    const float *Ahi, *Alo, *Bhi, *Blo;
+    double *C;
+    const double *Cadd;
+    const GemmPair *pairs;
+    const GemmOut *outs;
+    const GemmTile *tiles;
+    int32_t ntiles, pad;
+    double alpha, beta;
+};
+void launch_gemm_tc(const TcArgs &a, int mode);
 int gemm_tile_m(int mode);
 int gemm_tile_n(int mode);
 
