@@ -21,7 +21,7 @@ namespace cg = cooperative_groups;
 namespace qtt {
 namespace {
 constexpr int JT = 256;   // threads per CTA of the packing kernels
-constexpr int JJ = 1024;  // threads per CTA of the Jacobi kernel: one CTA per SM keeps the grid barrier cheap
+constexpr int JJ = 256;   // threads per CTA of the Jacobi kernel
 
 template <class T>
 __device__ __forceinline__ T wsum(T v) {
@@ -126,11 +126,93 @@ struct JacobiParams {
     int *rotated;  // nsec * max_sweeps flags, zero on entry: a rotation happened in (sector, sweep)
 };
 
+// Rotation of one column pair by one warp.  With R > 0 (p <= 32 R) every lane
+// first loads its R elements of both columns into registers -- one round trip to
+// L2 instead of one per element -- then forms the three inner products, the
+// rotation, and writes back from registers; the rotation-matrix columns follow
+// the same pattern.  R == 0 streams columns of any length.  Returns whether a
+// rotation was applied.
+template <class T, int R>
+__device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ wb, T *__restrict__ va,
+                                            T *__restrict__ vb, int p, int q, int lane) {
+    T al = 0, be = 0, ga = 0;
+    T x[R > 0 ? R : 1], y[R > 0 ? R : 1];
+    if (R > 0) {
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int r = lane + 32 * i;
+            x[i] = r < p ? ldcg(wa + r) : T(0);
+            y[i] = r < p ? ldcg(wb + r) : T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            al = fma(x[i], x[i], al);
+            be = fma(y[i], y[i], be);
+            ga = fma(x[i], y[i], ga);
+        }
+    } else {
+        for (int r = lane; r < p; r += 32) {
+            T xx = ldcg(wa + r), yy = ldcg(wb + r);
+            al = fma(xx, xx, al);
+            be = fma(yy, yy, be);
+            ga = fma(xx, yy, ga);
+        }
+    }
+    al = wsum(al);
+    be = wsum(be);
+    ga = wsum(ga);
+    if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
+    const T zeta = (be - al) / (T(2) * ga);
+    T t;
+    if (fabs(zeta) > T(1e18))
+        t = T(0.5) / zeta;
+    else
+        t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+    const T c = T(1) / sqrt(T(1) + t * t);
+    const T sn = c * t;
+    if (R > 0) {
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int r = lane + 32 * i;
+            if (r < p) {
+                wa[r] = c * x[i] - sn * y[i];
+                wb[r] = sn * x[i] + c * y[i];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int r = lane + 32 * i;
+            x[i] = r < q ? ldcg(va + r) : T(0);
+            y[i] = r < q ? ldcg(vb + r) : T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int r = lane + 32 * i;
+            if (r < q) {
+                va[r] = c * x[i] - sn * y[i];
+                vb[r] = sn * x[i] + c * y[i];
+            }
+        }
+    } else {
+        for (int r = lane; r < p; r += 32) {
+            T xx = ldcg(wa + r), yy = ldcg(wb + r);
+            wa[r] = c * xx - sn * yy;
+            wb[r] = sn * xx + c * yy;
+        }
+        for (int r = lane; r < q; r += 32) {
+            T xx = ldcg(va + r), yy = ldcg(vb + r);
+            va[r] = c * xx - sn * yy;
+            vb[r] = sn * xx + c * yy;
+        }
+    }
+    return true;
+}
+
 // One grid barrier per step.  Every CTA keeps its own copy of the per-sector
 // sweep / done state in shared memory and updates it identically after each
 // barrier from the rotation flags, so no second barrier is needed to publish it.
-template <class T>
-__global__ void __launch_bounds__(JJ, 1) k_jacobi(JacobiParams<T> P) {
+template <class T, int R>
+__global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ int jsh[];
     const int nsec = P.nsec;
@@ -184,37 +266,9 @@ __global__ void __launch_bounds__(JJ, 1) k_jacobi(JacobiParams<T> P) {
             }
             T *wa = P.work + sd.w_off + int64_t(a) * sd.p;
             T *wb = P.work + sd.w_off + int64_t(b) * sd.p;
-            T al = 0, be = 0, ga = 0;
-            for (int r = lane; r < sd.p; r += 32) {
-                T x = ldcg(wa + r), y = ldcg(wb + r);
-                al = fma(x, x, al);
-                be = fma(y, y, be);
-                ga = fma(x, y, ga);
-            }
-            al = wsum(al);
-            be = wsum(be);
-            ga = wsum(ga);
-            if (ga == T(0) || fabs(ga) <= Eps<T>::tol(sd.p) * sqrt(al) * sqrt(be)) continue;
-            const T zeta = (be - al) / (T(2) * ga);
-            T t;
-            if (fabs(zeta) > T(1e18))
-                t = T(0.5) / zeta;
-            else
-                t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-            const T c = T(1) / sqrt(T(1) + t * t);
-            const T sn = c * t;
-            for (int r = lane; r < sd.p; r += 32) {
-                T x = ldcg(wa + r), y = ldcg(wb + r);
-                wa[r] = c * x - sn * y;
-                wb[r] = sn * x + c * y;
-            }
             T *va = P.rot + sd.rot_off + int64_t(a) * sd.q;
             T *vb = P.rot + sd.rot_off + int64_t(b) * sd.q;
-            for (int r = lane; r < sd.q; r += 32) {
-                T x = ldcg(va + r), y = ldcg(vb + r);
-                va[r] = c * x - sn * y;
-                vb[r] = sn * x + c * y;
-            }
+            if (!rotate_pair<T, R>(wa, wb, va, vb, sd.p, sd.q, lane)) continue;
             if (lane == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
         }
         grid.sync();
@@ -350,23 +404,32 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
     }
 }
 
+template <class T, int R>
+void jacobi_launch(const JacobiParams<T> &P, size_t smem) {
+    static int nsm = 0;
+    static int per_sm = 0;
+    if (!nsm) {
+        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx().device), "SM count");
+        cuda_check(cudaFuncSetAttribute(k_jacobi<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
+                   "Jacobi smem attribute");
+    }
+    int occ = 0;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_jacobi<T, R>, JJ, smem), "occupancy");
+    if (occ < 1) fail(ERR_RUNTIME, "the Jacobi kernel cannot be resident on an SM");
+    per_sm = std::min(occ, 4);
+    JacobiParams<T> Pc = P;
+    void *args[] = {&Pc};
+    dim3 grid(nsm * per_sm), block(JJ);
+    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi<T, R>, grid, block, args, smem, ctx().stream),
+               "cooperative Jacobi launch");
+    count_launch();
+}
+
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
-                 int max_sweeps, int *sweeps_out, int *flags) {
-    static int nsm = 0;
-    static bool attr = false;
-    if (!nsm) cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx().device), "SM count");
-    if (!attr) {
-        cuda_check(cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
-                   "Jacobi smem attribute");
-        attr = true;
-    }
+                 int max_sweeps, int *sweeps_out, int *flags, int max_p) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
-    int per_sm = 0;
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi<T>, JJ, smem), "occupancy");
-    if (per_sm < 1) fail(ERR_RUNTIME, "the Jacobi kernel cannot be resident on an SM");
-    per_sm = 1;
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), ctx().stream), "memset flags");
     JacobiParams<T> P;
     P.work = work;
@@ -378,11 +441,17 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     P.max_steps = int64_t(max_sweeps) * std::max(1, max_steps_per_sweep) + 1;
     P.sweeps = sweeps_out;
     P.rotated = flags;
-    void *args[] = {&P};
-    dim3 grid(nsm * per_sm), block(JJ);
-    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi<T>, grid, block, args, smem, ctx().stream),
-               "cooperative Jacobi launch");
-    count_launch();
+    // registers per lane: the longest column over the sectors decides
+    if (max_p <= 4 * 32)
+        jacobi_launch<T, 4>(P, smem);
+    else if (max_p <= 8 * 32)
+        jacobi_launch<T, 8>(P, smem);
+    else if (max_p <= 16 * 32)
+        jacobi_launch<T, 16>(P, smem);
+    else if (max_p <= 32 * 32)
+        jacobi_launch<T, 32>(P, smem);
+    else
+        jacobi_launch<T, 0>(P, smem);
 }
 
 template <class T>
@@ -424,14 +493,14 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 }
 
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32) {
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p) {
     if (nsec <= 0) return;
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
-                    max_sweeps, sweeps_out, flags);
+                    max_sweeps, sweeps_out, flags, max_p);
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
-                    max_steps_per_sweep, max_sweeps, sweeps_out, flags);
+                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p);
 }
 
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,

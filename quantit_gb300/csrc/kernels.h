@@ -155,7 +155,7 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 // sweeps_out[s] receives the number of sweeps sector s used; flags holds
 // nsec*max_sweeps ints of scratch.
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32);
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p);
 // Column norms, sort (descending for svd, ascending eigenvalues for eigh),
 // normalisation and completion of null columns; writes U (m x k), V (n x k)
 // column-major and s (k) per sector in FP64, k = min(m, n).  max_q: largest q;

@@ -160,7 +160,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     require_f64(t);
     const int r = t.rank;
     int64_t wtot = 0, rtot = 0, utot = 0, vtot = 0, stot = 0;
-    int max_q = 0, max_steps = 1;
+    int max_q = 0, max_p = 0, max_steps = 1;
     std::vector<int> slots(1, 0);
     for (size_t g = 0; g < D.secs.size(); ++g) {
         const Sector &s = D.secs[g];
@@ -185,6 +185,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             vtot += int64_t(d.n) * d.q;
             stot += d.q;
             max_q = std::max(max_q, int(d.q));
+            max_p = std::max(max_p, int(d.p));
             int qp = d.q + (d.q & 1);
             if (qp >= 2) max_steps = std::max(max_steps, qp - 1);
             slots.push_back(slots.back() + qp / 2);
@@ -246,7 +247,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     BufPtr scratch = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
     {
         StatScope sc(ST_SVD, est);
-        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32);
+        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p);
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
                       static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32);
     }
