@@ -188,6 +188,24 @@ int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_d
  * (contract(bMPS, bMPS, bMPO) and contract(bMPS, bMPS), include/MPT.h; sources/MPT.cpp:211-290). */
 int qtt_mps_energy(int32_t L, const qtt_bt *mpo, const qtt_bt *mps, double *energy, double *norm2);
 
+/* ------------------------------------------------------------------ allocation-free SVD
+ * No counterpart in QuantiT: an addition for callers that cannot allocate device
+ * memory (inside a captured graph region, under a fixed memory budget, or when
+ * only pre-registered buffers may be used).  Thin SVD A = U diag(s) V^T of one
+ * dense FP64 matrix with the same one-sided Jacobi kernels as the sector SVD,
+ * using only a file-scope device array of QTT_SVD_NOALLOC_SCRATCH_BYTES (held by
+ * every GPU that loads the library until exit) -- no cudaMalloc / cudaFree.
+ *   a: m x n row-major (device), u: m x k row-major, s: k, v: n x k row-major
+ *   (device outputs), k = min(m, n), m and n <= QTT_SVD_NOALLOC_MAX_DIM; larger
+ *   sizes are rejected with QTT_ERR_INVALID_ARGUMENT.  Work is issued on `stream`
+ *   (a cudaStream_t, NULL = legacy default stream) and is asynchronous.
+ * The first call on a device looks up the scratch array's device address; make
+ * that first call outside any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU race and corrupt each other's results. */
+#define QTT_SVD_NOALLOC_MAX_DIM 256
+#define QTT_SVD_NOALLOC_SCRATCH_BYTES (5u * 256u * 256u * 8u + 2048u)
+int qtt_svd_dense_noalloc(const double *a, int64_t m, int64_t n, double *u, double *s, double *v, void *stream);
+
 /* ------------------------------------------------------------------ measurement */
 /* Per-kernel-class device time (CUDA events on the launching stream) and
  * algorithmic work: kind 0 block GEMM (FLOP), 1 permute (bytes), 2 sector SVD

@@ -33,6 +33,13 @@ int guarded(F &&f) {
     }
 }
 
+}  // namespace
+
+namespace qtt {
+void set_last_error(const std::string &msg) { tl_err = msg; }
+}  // namespace qtt
+
+namespace {
 qtt::BT &T(qtt_bt h) {
     if (!h) qtt::fail(qtt::ERR_INVALID_ARGUMENT, "null btensor handle");
     return h->t;

@@ -405,11 +405,13 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
 }
 
 template <class T, int R>
-void jacobi_launch(const JacobiParams<T> &P, size_t smem) {
+void jacobi_launch(const JacobiParams<T> &P, size_t smem, cudaStream_t stream) {
     static int nsm = 0;
     static int per_sm = 0;
     if (!nsm) {
-        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx().device), "SM count");
+        int dev = 0;
+        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
         cuda_check(cudaFuncSetAttribute(k_jacobi<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
                    "Jacobi smem attribute");
     }
@@ -420,17 +422,17 @@ void jacobi_launch(const JacobiParams<T> &P, size_t smem) {
     JacobiParams<T> Pc = P;
     void *args[] = {&Pc};
     dim3 grid(nsm * per_sm), block(JJ);
-    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi<T, R>, grid, block, args, smem, ctx().stream),
+    cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi<T, R>, grid, block, args, smem, stream),
                "cooperative Jacobi launch");
     count_launch();
 }
 
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
-                 int max_sweeps, int *sweeps_out, int *flags, int max_p) {
+                 int max_sweeps, int *sweeps_out, int *flags, int max_p, cudaStream_t stream) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
-    cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), ctx().stream), "memset flags");
+    cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
     JacobiParams<T> P;
     P.work = work;
     P.rot = rot;
@@ -443,20 +445,20 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     P.rotated = flags;
     // registers per lane: the longest column over the sectors decides
     if (max_p <= 4 * 32)
-        jacobi_launch<T, 4>(P, smem);
+        jacobi_launch<T, 4>(P, smem, stream);
     else if (max_p <= 8 * 32)
-        jacobi_launch<T, 8>(P, smem);
+        jacobi_launch<T, 8>(P, smem, stream);
     else if (max_p <= 16 * 32)
-        jacobi_launch<T, 16>(P, smem);
+        jacobi_launch<T, 16>(P, smem, stream);
     else if (max_p <= 32 * 32)
-        jacobi_launch<T, 32>(P, smem);
+        jacobi_launch<T, 32>(P, smem, stream);
     else
-        jacobi_launch<T, 0>(P, smem);
+        jacobi_launch<T, 0>(P, smem, stream);
 }
 
 template <class T>
 void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
-                 int max_q, double *scratch) {
+                 int max_q, double *scratch, cudaStream_t stream) {
     size_t smem = size_t(max_q) * (sizeof(double) + sizeof(int)) + 16;
     static bool attr = false;
     if (!attr) {
@@ -465,7 +467,7 @@ void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, c
         attr = true;
     }
     if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the SVD finishing kernel");
-    k_finish<T><<<nsec, 1024, smem, ctx().stream>>>(work, rot, U, V, s, sec, scratch);
+    k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch);
     count_launch();
     cuda_check(cudaGetLastError(), "SVD finishing kernel launch");
 }
@@ -492,26 +494,38 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
     cuda_check(cudaGetLastError(), "eigh prepare kernel launch");
 }
 
-void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p) {
+void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
+                      int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
+                      int max_p) {
     if (nsec <= 0) return;
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
-                    max_sweeps, sweeps_out, flags, max_p);
+                    max_sweeps, sweeps_out, flags, max_p, stream);
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
-                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p);
+                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, stream);
+}
+
+void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p) {
+    launch_jacobi_on(ctx().stream, work, rot, sec, slot_start, nsec, max_steps_per_sweep, max_sweeps, sweeps_out, flags,
+                     f32, max_p);
+}
+
+void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
+                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32) {
+    if (nsec <= 0) return;
+    if (f32)
+        finish_impl(static_cast<const float *>(work), static_cast<const float *>(rot), U, V, s, sec, nsec, max_q,
+                    scratch, stream);
+    else
+        finish_impl(static_cast<const double *>(work), static_cast<const double *>(rot), U, V, s, sec, nsec, max_q,
+                    scratch, stream);
 }
 
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
                    int max_q, double *scratch, int f32) {
-    if (nsec <= 0) return;
-    if (f32)
-        finish_impl(static_cast<const float *>(work), static_cast<const float *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch);
-    else
-        finish_impl(static_cast<const double *>(work), static_cast<const double *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch);
+    launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32);
 }
 
 }  // namespace qtt

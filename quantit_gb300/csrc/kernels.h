@@ -162,6 +162,12 @@ void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot
 // scratch: FP64 buffer with the work buffer's element offsets.
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec,
                    int nsec, int max_q, double *scratch, int f32);
+// The same two launches on an explicit stream (no library context involved).
+void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
+                      int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
+                      int max_p);
+void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
+                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32);
 // Segment = one output block (rows x k row-major at dst_off) from a column-major
 // (ld x *) sector matrix at src_off: dst[i*k + j] = src[src_off + (r0 + i) + j*ld].
 struct ScatterEntry {
