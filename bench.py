@@ -8,11 +8,14 @@ full sweep (2(L-2) bond updates).  Synthetic data: no dataset is involved.
 
 Arms:
   (default)          our CUDA path through libqtt_gb300.so (qtt_dmrg); block GEMMs
-                     in --mode (f64 = the plain drop-in, tf32x3 / bf16x3 = split
-                     precision on tcgen05); FP64 everywhere else.
+                     in --mode (tf32x3 = split TF32 on tcgen05 tensor cores with an
+                     FP32 sector SVD -- the mixed path; f64 = the plain drop-in).
+                     With --compare-f64 the plain FP64 path runs the same number of
+                     sweeps from the same state; both final states are evaluated in
+                     FP64 (<psi|H|psi>/<psi|psi>) for |dE| per site.
   --impl reference   the CPU oracle (numpy restatement of QuantiT's algorithm) on
-                     the host cores, each step a bounded sample of bond updates
-                     extrapolated to a sweep.
+                     the host cores; each step is one mid-chain bond update at D,
+                     extrapolated to a sweep by the sweep's size-weighted bond count.
 
 Prints one JSON line (rank 0).  Multi-GPU (torchrun) runs independent replicas,
 one solve per GPU ("replicas only": a DMRG sweep is sequential).
@@ -42,18 +45,15 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--L", type=int, default=32)
     p.add_argument("--D", type=int, default=2048)
-    p.add_argument("--mode", default="f64", choices=["f64", "tf32x3", "bf16x3"])
+    p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
-    p.add_argument("--cpu-sample-bonds", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
 
 
 class ClockSampler:
@@ -113,13 +113,13 @@ def build_state(q, L, D, seed=0):
     return mpo, mps
 
 
-def run_sweeps(q, mpo, mps, n, mode, stream_events=True):
-    """n single sweeps; returns (energies, per-sweep seconds, final mps) timed with CUDA
-    events on the library's stream."""
+def run_sweeps(q, mpo, mps, n, mode, D):
+    """n single sweeps timed with CUDA events on the library's stream; the Ritz
+    energy of each sweep and the final state."""
     import torch
     stream = torch.cuda.ExternalStream(q.lib().qtt_get_stream())
-    opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=DMAX[0], min_bond=4,
-                                     maximum_iterations=1, gemm=mode)
+    opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4,
+                                     maximum_iterations=1, gemm=mode, final_energy_fp64=False)
     cur = q.networks.bMPS(list(mps), mps.orthogonality_center)
     Es, ts = [], []
     for _ in range(n):
@@ -135,15 +135,19 @@ def run_sweeps(q, mpo, mps, n, mode, stream_events=True):
     return Es, ts, cur
 
 
-DMAX = [2048]
+def fp64_energy(q, mpo, mps):
+    t0 = time.perf_counter()
+    e, n2 = q.algorithms.mps_energy(mpo, mps)
+    return e / n2, time.perf_counter() - t0
 
 
-def fp64_peak_tflops():
-    """cuBLAS DGEMM throughput measured here (the FP64 roofline denominator)."""
+def matmul_peak_tflops(dtype, tf32=False):
+    """cuBLAS GEMM throughput measured in this run (FP64 / FP32 SIMT denominators)."""
     import torch
+    torch.backends.cuda.matmul.allow_tf32 = tf32
     n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
     for _ in range(2):
         a @ b
     torch.cuda.synchronize()
@@ -158,67 +162,116 @@ def fp64_peak_tflops():
     return 2 * n ** 3 / best / 1e12
 
 
-def cpu_baseline(L, D, sample_bonds):
-    """The oracle (numpy; BLAS threads = all host cores) on a bounded sample: a few
-    mid-chain bond updates at bond dimension D, extrapolated to a sweep."""
-    from oracle import qtt_oracle as o
-    rng = np.random.default_rng(0)
-    mpo = o.heisenberg_mpo(L)
-    mps = o.random_mps(L, D, [1, -1], 0, rng)
-    mid = L // 2 - 1
-    # a right-canonical right half and a left-canonical left half are not needed for
-    # timing: the work of a bond update depends only on the block shapes
-    env = [None] * (L + 2)
-    env[0] = o.trivial_edge((mps[0], 0), (mpo[0], 0))
-    env[L + 1] = o.trivial_edge((mps[-1], 2), (mpo[-1], 2))
-    for i in range(mid):
-        env[i + 1] = o.compute_left_env(mpo[i], mps[i], env[i])
-    for i in range(L - 1, mid + 1, -1):
-        env[i + 1] = o.compute_right_env(mpo[i], mps[i], env[i + 2])
-    h2 = o.compute_2sites_hamil(mpo)
-    opts = o.DmrgOptions(cutoff=1e-10, maximum_bond=D, minimum_bond=4)
+class CpuSampler:
+    """The oracle (numpy; BLAS on all host cores) at the workload's mid-chain bond:
+    environments are built once, each sample is one two-site bond update at D."""
+
+    def __init__(self, L, D):
+        from oracle import qtt_oracle as o
+        self.o, self.L, self.D = o, L, D
+        rng = np.random.default_rng(0)
+        self.mpo = o.heisenberg_mpo(L)
+        self.mps = o.random_mps(L, D, [1, -1], 0, rng)
+        self.mid = L // 2 - 1
+        env = [None] * (L + 2)
+        env[0] = o.trivial_edge((self.mps[0], 0), (self.mpo[0], 0))
+        env[L + 1] = o.trivial_edge((self.mps[-1], 2), (self.mpo[-1], 2))
+        for i in range(self.mid):
+            env[i + 1] = o.compute_left_env(self.mpo[i], self.mps[i], env[i])
+        for i in range(L - 1, self.mid + 1, -1):
+            env[i + 1] = o.compute_right_env(self.mpo[i], self.mps[i], env[i + 2])
+        self.env = env
+        self.h2 = o.compute_2sites_hamil(self.mpo)
+        self.opts = o.DmrgOptions(cutoff=1e-10, maximum_bond=D, minimum_bond=4)
+        # bonds of a sweep weighted by their cost relative to the mid bond (sum over sectors of D_b^3)
+        from quantit_gb300.networks import bond_sectors  # pure-python structure helper
+        bonds = bond_sectors(L, D, [1, -1], 0)
+        w = [sum(m ** 3 for m in b.values()) for b in bonds]
+        sweep_bonds = list(range(0, L - 2)) + list(range(L - 2, 0, -1))
+        self.factor = sum(w[b] / w[self.mid] for b in sweep_bonds)
+
+    def bond(self):
+        mps = [m for m in self.mps]
+        env = list(self.env)
+        t0 = time.perf_counter()
+        self.o.dmrg_bond_update(self.mpo, self.h2, mps, env, self.mid, True, self.opts)
+        return time.perf_counter() - t0
+
+
+def reference_arm(args, cfg):
+    """Each step = one mid-chain bond update of the oracle, extrapolated to a sweep."""
+    s = CpuSampler(args.L, args.D)
+    for _ in range(min(args.warmup, 1)):
+        s.bond()
+    per = [s.bond() for _ in range(args.steps)]
+    t_sweep = float(np.mean(per)) * s.factor
+    ncores = os.cpu_count()
+    sample = (f"{args.steps} mid-chain bond update(s) at D={args.D} ({np.mean(per):.2f} s each) "
+              f"x {s.factor:.1f} size-weighted bonds per sweep")
+    return {"metric": METRIC, "value": t_sweep, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_sweep * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": t_sweep, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample},
+            "e2e": {"value": t_sweep, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def roofline(kind, st, P, mode, peaks_cache):
+    """Achieved algorithmic throughput of one kernel class against its roofline."""
+    if st["ms"] <= 0:
+        return None
+    sec = st["ms"] / 1e3
+    base = {"kernel": kind, "per_launch_ms": st["ms"] / max(st["launches"], 1), "launches": st["launches"],
+            "traffic": None}
+    if kind == "gemm" and mode != "f64":
+        tf32 = P.get("bf16_tflops", 1939.7) / 2.0
+        ach = st["work"] / sec / 1e12
+        return dict(base, bound="tensor", achieved=ach, peak=tf32, unit="TFLOP/s", frac=ach / tf32,
+                    tensor_ops_frac=3.0 * ach / tf32,
+                    peak_source="dense TF32 = 1/2 of MEASURED_PEAKS.json bf16_tflops (of measured); "
+                                "achieved counts useful FLOP, the split issues 3 tensor products each")
+    if kind in ("gemm", "svd"):
+        fp32 = kind == "svd" and mode != "f64"
+        key = "fp32" if fp32 else "fp64"
+        if key not in peaks_cache:
+            import torch
+            peaks_cache[key] = matmul_peak_tflops(torch.float32 if fp32 else torch.float64)
+        ach = st["work"] / sec / 1e12
+        return dict(base, bound="latency (one grid barrier per Jacobi step)" if kind == "svd" else "fp64",
+                    achieved=ach, peak=peaks_cache[key], unit="TFLOP/s", frac=ach / peaks_cache[key],
+                    peak_source=f"cuBLAS {'SGEMM' if fp32 else 'DGEMM'} measured in this run")
+    ach = st["work"] / sec / 1e9
+    peak = P.get("hbm_gbs", 6800.0)
+    return dict(base, bound="hbm", achieved=ach, peak=peak, unit="GB/s", frac=ach / peak,
+                peak_source="MEASURED_PEAKS.json hbm_gbs (of measured)")
+
+
+def e2e_sweep(q, mpo, mps, args):
+    """One sweep through the public API with the MPS uploaded from host buffers and
+    the optimised MPS + energy read back to the host inside the timed region."""
+    host = [(t.copy_structure(), t.blocks()) for t in mps]
+    h2d = sum(sum(v.nbytes for _, v in blks) for _, blks in host)
+    opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=args.D, min_bond=4,
+                                     maximum_iterations=1, gemm=args.mode, final_energy_fp64=False)
     t0 = time.perf_counter()
-    done = 0
-    for k in range(sample_bonds):
-        o.dmrg_bond_update(mpo, h2, mps, env, mid, True, opts)
-        done += 1
-        if time.perf_counter() - t0 > 30:
-            break
-        mps_mid = mid  # stay on the same bond: redo the update from the new state
-    per_bond = (time.perf_counter() - t0) / done
-    # bonds of a sweep weighted by their size relative to the mid bond (Sigma D_b^3 / D_mid^3)
-    from quantit_gb300.networks import bond_sectors  # pure-python structure helper
-    bonds = bond_sectors(L, D, [1, -1], 0)
-    w = [sum(m ** 3 for m in b.values()) for b in bonds]
-    wm = w[mid]
-    sweep_bonds = list(range(0, L - 2)) + list(range(L - 2, 0, -1))
-    factor = sum(w[b] / wm for b in sweep_bonds)
-    return per_bond * factor, per_bond, done, factor
+    dev = q.networks.bMPS([s.set_blocks(b) for s, b in host], 0)
+    E = q.algorithms.dmrg(mpo, dev, opts)
+    out = [t.blocks() for t in dev]
+    dt = time.perf_counter() - t0
+    d2h = sum(sum(v.nbytes for _, v in blks) for blks in out) + 8
+    return {"value": dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "E": E}
 
 
 def main():
     args = parse()
     rank, world, local = dist_env()
-    DMAX[0] = args.D
     cfg = {"workload": f"Heisenberg chain L={args.L}, two-site DMRG sweep at D={args.D}, U(1) Sz=0",
            "L": args.L, "D": args.D, "model": "spin-1/2 Heisenberg open chain (J=1 AFM)",
            "cutoff": 1e-10, "update": "one-step Lanczos (QuantiT two_sites_update)",
            "l2": "working set (MPS + environments) far larger than L2 (129 MB)",
            "parallelism": "replicas only" if world > 1 else "single GPU"}
     if args.impl == "reference":
-        if rank != 0:
-            return
-        t_sweep, per_bond, n, factor = cpu_baseline(args.L, args.D, args.cpu_sample_bonds)
-        ncores = os.cpu_count()
-        line = {"metric": METRIC, "value": t_sweep, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": t_sweep * 1e3, "higher_is_better": False,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-                "impl": "reference",
-                "cpu_baseline": {"value": t_sweep, "unit": UNIT, "cores": ncores, "kind": "port",
-                                 "sample": f"{n} mid-chain bond update(s) at D={args.D} ({per_bond:.2f} s each) "
-                                           f"x {factor:.1f} size-weighted bonds per sweep"},
-                "e2e": {"value": t_sweep, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        if rank == 0:
+            print(json.dumps(reference_arm(args, cfg)))
         return
 
     import torch
@@ -229,8 +282,7 @@ def main():
     import quantit_gb300 as q
     q.ensure_init(local)
     mpo, mps0 = build_state(q, args.L, args.D, seed=rank)
-    # warm-up sweeps in the measured mode
-    _, _, mps1 = run_sweeps(q, mpo, mps0, args.warmup, args.mode)
+    _, _, mps1 = run_sweeps(q, mpo, mps0, args.warmup, args.mode, args.D)
     q.stats.reset()
     q.stats.enable(True)
     sampler = ClockSampler(local)
@@ -240,7 +292,7 @@ def main():
     launches0 = q.stats.launches()
     sampler.start()
     t0 = time.perf_counter()
-    Es, ts, _ = run_sweeps(q, mpo, mps1, args.steps, args.mode)
+    Es, ts, mps2 = run_sweeps(q, mpo, mps1, args.steps, args.mode, args.D)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
@@ -249,83 +301,46 @@ def main():
     q.stats.enable(False)
     t_step = float(np.mean(ts))
     if world > 1:
-        t = torch.tensor([wall], device="cuda")
+        t = torch.tensor([wall, t_step], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall = float(t.item())
-    # FP64 plain comparison from the same state
+        wall, t_step = float(t[0].item()), float(t[1].item())
+    E_mixed, t_eval = fp64_energy(q, mpo, mps2)
     cmp = None
     if args.mode != "f64" and args.compare_f64:
-        E64, t64, _ = run_sweeps(q, mpo, mps1, args.steps, "f64")
+        _, t64, mps64 = run_sweeps(q, mpo, mps1, args.steps, "f64", args.D)
+        E64, _ = fp64_energy(q, mpo, mps64)
         cmp = {"fp64_s_per_sweep": float(np.mean(t64)), "speedup_vs_fp64": float(np.mean(t64)) / t_step,
-               "dE_per_site": abs(Es[-1] - E64[-1]) / args.L, "E_fp64": E64[-1]}
-    # e2e: one sweep through the C-ABI from host buffers, results back to the host
+               "dE_per_site": abs(E_mixed - E64) / args.L, "E_fp64": E64, "E_mixed": E_mixed,
+               "energies": "FP64 <psi|H|psi>/<psi|psi> of each path's final state after the same sweeps"}
     e2e = e2e_sweep(q, mpo, mps1, args)
-    # roofline for the dominant kernel class
-    dom = max(kinds, key=lambda k: kinds[k]["ms"])
     P = peaks()
-    roof = roofline(dom, kinds[dom], P)
+    pc = {}
+    dom = max(kinds, key=lambda k: kinds[k]["ms"])
     line = {"metric": METRIC, "value": t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f64",
-            "data": "synthetic", "config": dict(cfg, mode=args.mode), "energies": Es,
-            "energy_per_site": Es[-1] / args.L, "sweep_times_s": ts, "wall_s": wall,
-            "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()}, "roofline": roof,
+            "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f32svd+f64",
+            "data": "synthetic", "config": dict(cfg, mode=args.mode), "ritz_energies": Es,
+            "energy_fp64": E_mixed, "energy_per_site": E_mixed / args.L, "fp64_energy_eval_s": t_eval,
+            "sweep_times_s": ts, "wall_s": wall, "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()},
+            "roofline": roofline(dom, kinds[dom], P, args.mode, pc),
+            "roofline_gemm": roofline("gemm", kinds["gemm"], P, args.mode, pc),
             "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e}
     if cmp:
         line["vs_fp64"] = cmp
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            t_sweep, per_bond, n, factor = cpu_baseline(args.L, args.D, args.cpu_sample_bonds)
-            line["cpu_baseline"] = {"value": t_sweep, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                    "sample": f"{n} mid-chain bond update(s) at D={args.D} ({per_bond:.2f} s each) "
-                                              f"x {factor:.1f} size-weighted bonds per sweep"}
-        except Exception as e:  # report, never hide
+            s = CpuSampler(args.L, args.D)
+            per = [s.bond() for _ in range(2)]
+            line["cpu_baseline"] = {"value": float(np.mean(per)) * s.factor, "unit": UNIT, "cores": os.cpu_count(),
+                                    "kind": "port",
+                                    "sample": f"2 mid-chain bond updates at D={args.D} ({np.mean(per):.2f} s each) "
+                                              f"x {s.factor:.1f} size-weighted bonds per sweep"}
+        except Exception as e:  # reported, never hidden
             line["cpu_baseline"] = {"error": repr(e)}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
-
-
-def roofline(kind, st, P):
-    if st["ms"] <= 0:
-        return None
-    per_launch_ms = st["ms"] / max(st["launches"], 1)
-    if kind in ("gemm", "svd"):
-        mode_tc = False
-        achieved = st["work"] / (st["ms"] / 1e3) / 1e12
-        peak = P.get("fp64_tflops")
-        src = "FP64 peak (cuBLAS DGEMM, measured in this run)"
-        try:
-            peak = fp64_peak_tflops()
-        except Exception:
-            peak = 1.25
-            src = "FP64 nominal 1.25 TFLOP/s (fallback)"
-        return {"kernel": kind, "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "peak_source": src,
-                "per_launch_ms": per_launch_ms, "launches": st["launches"]}
-    achieved = st["work"] / (st["ms"] / 1e3) / 1e9
-    peak = P.get("hbm_gbs", 6800.0)
-    return {"kernel": kind, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs",
-            "per_launch_ms": per_launch_ms, "launches": st["launches"]}
-
-
-def e2e_sweep(q, mpo, mps, args):
-    """One sweep through the public API with the MPS uploaded from host buffers and
-    the optimised MPS + energy read back to the host inside the timed region."""
-    host = [(t.copy_structure(), t.blocks()) for t in mps]
-    h2d = sum(sum(v.nbytes for _, v in blks) for _, blks in host)
-    t0 = time.perf_counter()
-    dev = q.networks.bMPS([shape.set_blocks(blks) for shape, blks in
-                           [(s.copy_structure(), b) for s, b in host]], 0)
-    opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=args.D, min_bond=4,
-                                     maximum_iterations=1, gemm=args.mode)
-    E = q.algorithms.dmrg(mpo, dev, opts)
-    out = [t.blocks() for t in dev]
-    dt = time.perf_counter() - t0
-    d2h = sum(sum(v.nbytes for _, v in blks) for blks in out) + 8
-    return {"value": dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "E": E}
 
 
 if __name__ == "__main__":

@@ -242,11 +242,26 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     int *sweeps = static_cast<int *>(ibuf->p);
     int *flags = sweeps + nsec;
     last_sweeps() = {ibuf, nsec};
-    double est = 0;
-    for (auto &d : D.desc) est += 8.0 * double(d.q) * double(d.q) * (6.0 * d.p + 4.0 * d.q);
     BufPtr scratch = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
+    if (stats_enabled()) {
+        // algorithmic work: every pair evaluation of every sweep (dots 6p, rotation 6p, V 6q),
+        // resolved from the sweep counts when the statistics are read (no sync here)
+        std::vector<std::pair<int, int>> pq;
+        for (auto &d : D.desc) pq.push_back({d.p, d.q});
+        BufPtr keep = ibuf;
+        stats_defer_work(ST_SVD, [keep, pq, nsec]() {
+            std::vector<int> sw(nsec);
+            cuda_check(cudaMemcpy(sw.data(), keep->p, size_t(nsec) * sizeof(int), cudaMemcpyDeviceToHost),
+                       "read sweeps");
+            double w = 0;
+            for (int s = 0; s < nsec; ++s)
+                w += double(sw[s]) * 0.5 * double(pq[s].second) * double(pq[s].second - 1) *
+                     (12.0 * pq[s].first + 6.0 * pq[s].second);
+            return w;
+        });
+    }
     {
-        StatScope sc(ST_SVD, est);
+        StatScope sc(ST_SVD, 0.0);
         launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p);
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
                       static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32);

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -305,6 +306,8 @@ inline void tc_error_raise() {
 enum StatKind : int { ST_GEMM = 0, ST_PERMUTE = 1, ST_SVD = 2, ST_ELEMWISE = 3, ST_PACK = 4, ST_COUNT = 5 };
 void stats_enable(bool on);
 bool stats_enabled();
+// Work known only after the kernels ran (e.g. Jacobi sweeps): resolved when read.
+void stats_defer_work(int kind, std::function<double()> f);
 struct StatScope {
     int kind;
     double work;

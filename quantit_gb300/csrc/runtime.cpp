@@ -115,7 +115,11 @@ std::vector<Pending> g_pending;
 std::mutex g_stats_mu;
 std::atomic<int64_t> g_launches{0};
 
+std::vector<std::pair<int, std::function<double()>>> g_deferred;
+
 void drain_pending() {
+    for (auto &d : g_deferred) g_stats[d.first].work += d.second();
+    g_deferred.clear();
     for (auto &p : g_pending) {
         float ms = 0;
         cudaEventSynchronize(p.e1);
@@ -131,6 +135,10 @@ void drain_pending() {
 }  // namespace
 
 void stats_enable(bool on) { g_stats_on = on; }
+void stats_defer_work(int kind, std::function<double()> f) {
+    std::lock_guard<std::mutex> lk(g_stats_mu);
+    g_deferred.push_back({kind, std::move(f)});
+}
 bool stats_enabled() { return g_stats_on; }
 StatScope::StatScope(int k, double w) : kind(k), work(w) {
     if (!g_stats_on) return;
