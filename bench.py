@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--jacobi", default="block", choices=["block", "scalar"],
+                   help="sector-SVD Jacobi kernel (block-cyclic where it fits, or scalar)")
     return p.parse_args()
 
 
@@ -281,6 +283,7 @@ def main():
         dist.init_process_group("nccl")
     import quantit_gb300 as q
     q.ensure_init(local)
+    q.set_jacobi_kernel(args.jacobi)
     mpo, mps0 = build_state(q, args.L, args.D, seed=rank)
     _, _, mps1 = run_sweeps(q, mpo, mps0, args.warmup, args.mode, args.D)
     q.stats.reset()
@@ -319,7 +322,7 @@ def main():
     line = {"metric": METRIC, "value": t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f32svd+f64",
-            "data": "synthetic", "config": dict(cfg, mode=args.mode), "ritz_energies": Es,
+            "data": "synthetic", "config": dict(cfg, mode=args.mode, jacobi=args.jacobi), "ritz_energies": Es,
             "energy_fp64": E_mixed, "energy_per_site": E_mixed / args.L, "fp64_energy_eval_s": t_eval,
             "sweep_times_s": ts, "wall_s": wall, "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()},
             "roofline": roofline(dom, kinds[dom], P, args.mode, pc),

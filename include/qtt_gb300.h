@@ -66,6 +66,10 @@ int qtt_synchronize(void);
 /* Block-GEMM precision for the calling process (QTT_GEMM_*). */
 int qtt_set_gemm_mode(int mode);
 int qtt_get_gemm_mode(void);
+/* Sector-SVD kernel (no reference counterpart; a tuning and testing switch):
+ * 0 = block-cyclic Jacobi wherever the sector shapes fit it (default),
+ * 1 = scalar Jacobi (one column pair per warp and grid step) everywhere. */
+int qtt_set_jacobi_kernel(int which);
 
 /* ------------------------------------------------------------------ btensor
  * btensor(index_list sections_by_dim, any_quantity_vector c_vals, index_list

@@ -19,6 +19,13 @@ def set_gemm_mode(mode):
     call("qtt_set_gemm_mode", algorithms.GEMM_MODES[mode] if isinstance(mode, str) else int(mode))
 
 
+def set_jacobi_kernel(which):
+    """Sector-SVD Jacobi kernel: 'block' (block-cyclic wherever it fits, the
+    default) or 'scalar' (one column pair per warp and grid step)."""
+    from ._lib import call
+    call("qtt_set_jacobi_kernel", {"block": 0, "scalar": 1}[which] if isinstance(which, str) else int(which))
+
+
 class stats:
     """Per-kernel-class device time (CUDA events) and algorithmic work."""
     KINDS = {"gemm": 0, "permute": 1, "svd": 2, "elementwise": 3, "pack": 4}

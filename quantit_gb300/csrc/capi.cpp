@@ -84,6 +84,9 @@ int qtt_set_gemm_mode(int mode) {
     return guarded([&] { qtt::set_gemm_mode(mode); });
 }
 int qtt_get_gemm_mode(void) { return qtt::gemm_mode(); }
+int qtt_set_jacobi_kernel(int which) {
+    return guarded([&] { qtt::set_jacobi_variant(which); });
+}
 
 int qtt_bt_create(int32_t rank, const int64_t *sbd, const int64_t *ssz, int32_t ncomp, const uint16_t *moduli,
                   const int16_t *c_vals, const int16_t *sel, int32_t dtype, qtt_bt *out) {

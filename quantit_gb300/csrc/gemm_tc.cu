@@ -14,12 +14,13 @@
 //    pipe is a small fraction of its FP32 / integer rate.
 //  * k_gemm_tf32x3: CTA = one 128 x 128 tile of one output block (same tile and
 //    pair tables as the FP64 kernel).  All 8 warps copy 16-byte vectors of the
-//    split operands into a 2-stage shared-memory ring in the canonical no-swizzle
+//    split operands into a 3-stage shared-memory ring in the canonical no-swizzle
 //    K-major UMMA layout (core matrices of 8 rows x 16 bytes).  Thread 0 issues
 //    the tcgen05.mma instructions of a stage (3 products x 4 k-steps of 8) and
 //    commits them to that stage's mbarrier, which the producers wait on before
 //    refilling the stage.  The epilogue reads the accumulator with tcgen05.ld and
-//    writes alpha*acc + beta*add in FP64.
+//    writes alpha*acc + beta*add in FP64 (a plain integer widening when alpha = 1
+//    and there is no add term).
 //
 // Every mbarrier wait is bounded; on timeout the kernel records an error code in
 // a device word that the host checks, still waits (bounded) for its MMAs and
@@ -38,7 +39,7 @@ constexpr int TMEM_COLS = 128;  // FP32 accumulator columns (N)
 constexpr int A_BYTES = TBM * TBK * 4;  // one operand copy: 16 KB
 constexpr int B_BYTES = TBN * TBK * 4;  // 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi/lo of A and B: 64 KB
-constexpr int NSTAGE = 2;
+constexpr int NSTAGE = 3;
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024;
 constexpr uint32_t LBO = 128;                   // K-adjacent core matrices
 constexpr uint32_t SBO = (TBK * 4 / 16) * 128;  // next 8-row group: 1024 B
@@ -111,6 +112,21 @@ __device__ __forceinline__ float f64_to_f32_int(double x) {
         }
     }
     return __uint_as_float(sign | f);
+}
+
+// FP32 -> FP64 (exact) with integer operations only; FP32 subnormals flush to zero.
+__device__ __forceinline__ double f32_to_f64_int(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+    const uint32_t e = (b >> 23) & 0xFF, m = b & 0x7FFFFF;
+    unsigned long long d;
+    if (e == 0)
+        d = sign;
+    else if (e == 0xFF)
+        d = sign | 0x7FF0000000000000ull | ((unsigned long long)m << 29);
+    else
+        d = sign | ((unsigned long long)(e - 127 + 1023) << 52) | ((unsigned long long)m << 29);
+    return __longlong_as_double(static_cast<long long>(d));
 }
 
 __global__ void k_split_tf32(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo,
@@ -206,7 +222,7 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
     for (int p = o.p0; p < o.p1; ++p) nchunk += ((g.pairs[p].K + 3) / 4 * 4 + TBK - 1) / TBK;
 
     int p = o.p0, k0 = 0;
-    uint32_t commits[NSTAGE] = {0, 0};
+    uint32_t commits[NSTAGE] = {};
     for (int c = 0; c < nchunk; ++c) {
         const int s = c % NSTAGE;
         if (c >= NSTAGE) {
@@ -285,13 +301,19 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
             for (int j = 0; j < 32; ++j) v[j] = 0u;
         }
         if (gm < o.M) {
+            // GB300's FP64 pipe is narrow: the plain case (alpha = 1, no add term) converts
+            // with integer operations only; FP64 arithmetic only for tensorgdot's epilogue
+            const bool plain = g.alpha == 1.0 && o.add_off < 0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 const int gn = t.n0 + col0 + j;
                 if (gn < o.N) {
                     const int64_t idx = int64_t(gm) * o.N + gn;
-                    double val = g.alpha * double(__uint_as_float(v[j]));
-                    if (o.add_off >= 0) val += g.beta * g.Cadd[o.add_off + idx];
+                    double val = f32_to_f64_int(__uint_as_float(v[j]));
+                    if (!plain) {
+                        val *= g.alpha;
+                        if (o.add_off >= 0) val += g.beta * g.Cadd[o.add_off + idx];
+                    }
                     g.C[o.c_off + idx] = val;
                 }
             }

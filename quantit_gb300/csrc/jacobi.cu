@@ -45,6 +45,33 @@ struct Eps<float> {
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 __device__ __forceinline__ float ldcg(const float *p) { return __ldcg(p); }
 
+// Plane rotation (c, s) applied in half-angle form with tau = s / (1 + c) = tan(theta/2):
+//     x' = x - s (y + tau x) = c x - s y,   y' = y + s (x - tau y) = s x + c y.
+// For small angles c rounds to 1 while 1 - c = s tau does not, so the plain form
+// c x - s y would scale both columns by sqrt(1 + t^2) at every such rotation; in
+// FP32 that bias accumulates to ~1e-5 in the singular values over a few sweeps.
+template <class T>
+__device__ __forceinline__ void rot_apply(T &x, T &y, T s, T tau) {
+    const T u = fma(tau, x, y);
+    const T v = fma(-tau, y, x);
+    x = fma(-s, u, x);
+    y = fma(s, v, y);
+}
+
+// Hestenes rotation for column norms al, be and inner product ga: s and tau.
+template <class T>
+__device__ __forceinline__ void rot_params(T al, T be, T ga, T &s, T &tau) {
+    const T zeta = (be - al) / (T(2) * ga);
+    T t;
+    if (fabs(zeta) > T(1e18))
+        t = T(0.5) / zeta;
+    else
+        t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+    const T c = T(1) / sqrt(T(1) + t * t);
+    s = c * t;
+    tau = s / (T(1) + c);
+}
+
 // Round-robin (circle method) pairing of qp (even) players at round k in [0, qp-1):
 // slot 0 pairs player 0 with 1 + k; slot i > 0 pairs 1 + (k+i) mod (qp-1) with 1 + (k-i) mod (qp-1).
 __device__ __forceinline__ void rr_pair(int qp, int k, int slot, int &a, int &b) {
@@ -162,21 +189,17 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
     be = wsum(be);
     ga = wsum(ga);
     if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
-    const T zeta = (be - al) / (T(2) * ga);
-    T t;
-    if (fabs(zeta) > T(1e18))
-        t = T(0.5) / zeta;
-    else
-        t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-    const T c = T(1) / sqrt(T(1) + t * t);
-    const T sn = c * t;
+    T sn, tau;
+    rot_params(al, be, ga, sn, tau);
     if (R > 0) {
 #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int r = lane + 32 * i;
             if (r < p) {
-                wa[r] = c * x[i] - sn * y[i];
-                wb[r] = sn * x[i] + c * y[i];
+                T xx = x[i], yy = y[i];
+                rot_apply(xx, yy, sn, tau);
+                wa[r] = xx;
+                wb[r] = yy;
             }
         }
 #pragma unroll
@@ -189,20 +212,24 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
         for (int i = 0; i < R; ++i) {
             const int r = lane + 32 * i;
             if (r < q) {
-                va[r] = c * x[i] - sn * y[i];
-                vb[r] = sn * x[i] + c * y[i];
+                T xx = x[i], yy = y[i];
+                rot_apply(xx, yy, sn, tau);
+                va[r] = xx;
+                vb[r] = yy;
             }
         }
     } else {
         for (int r = lane; r < p; r += 32) {
             T xx = ldcg(wa + r), yy = ldcg(wb + r);
-            wa[r] = c * xx - sn * yy;
-            wb[r] = sn * xx + c * yy;
+            rot_apply(xx, yy, sn, tau);
+            wa[r] = xx;
+            wb[r] = yy;
         }
         for (int r = lane; r < q; r += 32) {
             T xx = ldcg(va + r), yy = ldcg(vb + r);
-            va[r] = c * xx - sn * yy;
-            vb[r] = sn * xx + c * yy;
+            rot_apply(xx, yy, sn, tau);
+            va[r] = xx;
+            vb[r] = yy;
         }
     }
     return true;
@@ -290,6 +317,276 @@ __global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
     }
     if (blockIdx.x == 0)
         for (int s = threadIdx.x; s < nsec; s += blockDim.x) P.sweeps[s] = sweep[s];
+}
+
+// ---------------------------------------------------------------------------
+// Block-cyclic one-sided Jacobi.  The q columns of a sector are cut into blocks
+// of B columns; a grid step pairs the blocks round-robin (nbp - 1 steps per
+// sweep, nbp = blocks rounded up to even, a phantom block when odd) and one CTA
+// takes one block pair.  The CTA copies the 2B columns into shared memory and
+// runs, with CTA barriers only:
+//   * on the first step of a sweep, the B - 1 round-robin rounds inside each of
+//     the two blocks (every intra-block pair once per sweep);
+//   * the B rounds of inter-block pairs (I_k, J_(k+r) mod B): warp k keeps I_k in
+//     registers and the J columns move through shared memory.
+// Every column pair of the sector is thus visited exactly once per sweep, as in
+// the scalar ordering, but a sweep costs ~q/B grid barriers instead of ~q.  The
+// rotations of a step are accumulated into a 2B x 2B orthogonal matrix Q (one
+// element per lane and column) and applied to the rotation matrix V once at the
+// end of the step (V[:, I u J] <- V[:, I u J] Q).
+template <class T>
+struct BJacobiParams {
+    T *work;
+    T *rot;
+    const SectorDesc *secs;
+    int nsec;
+    int max_sweeps;
+    int64_t max_steps;
+    int *sweeps;   // per sector (written at the end)
+    int *rotated;  // nsec * max_sweeps flags, zero on entry
+};
+
+__device__ __forceinline__ int bj_items(int q, int B) {
+    if (q < 2) return 0;
+    const int nb = (q + B - 1) / B;
+    return (nb + (nb & 1)) / 2;
+}
+
+template <class T, int R>
+__device__ __forceinline__ void bj_load(T (&x)[R], const T *slot, int p, int lane) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int r = lane + 32 * i;
+        x[i] = r < p ? slot[r] : T(0);
+    }
+}
+
+template <class T, int R>
+__device__ __forceinline__ void bj_store(const T (&x)[R], T *slot, int p, int lane) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int r = lane + 32 * i;
+        if (r < p) slot[r] = x[i];
+    }
+}
+
+// Hestenes rotation of two register-resident columns (same test and formulas as
+// rotate_pair).  Returns whether a rotation was applied, with its s and tau.
+template <class T, int R>
+__device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], int p, T &sn, T &tau) {
+    T al = 0, be = 0, ga = 0;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        al = fma(x[i], x[i], al);
+        be = fma(y[i], y[i], be);
+        ga = fma(x[i], y[i], ga);
+    }
+    al = wsum(al);
+    be = wsum(be);
+    ga = wsum(ga);
+    if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
+    rot_params(al, be, ga, sn, tau);
+#pragma unroll
+    for (int i = 0; i < R; ++i) rot_apply(x[i], y[i], sn, tau);
+    return true;
+}
+
+template <class T, int B, int R>
+__global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
+    constexpr int NP = 2 * B;   // columns (players) of a block pair
+    constexpr int PP = 32 * R;  // shared-memory slot per column
+    constexpr int NT = 32 * B;
+    cg::grid_group grid = cg::this_grid();
+    extern __shared__ __align__(16) unsigned char bsh[];
+    T *cols = reinterpret_cast<T *>(bsh);  // NP slots of PP
+    T *Qs = cols + NP * PP;                // NP x NP, column-major
+    const int nsec = P.nsec;
+    int *done = reinterpret_cast<int *>(Qs + NP * NP);
+    int *sweep = done + nsec;
+    int *istart = sweep + nsec;  // nsec + 1 prefix sums of block pairs per step
+    __shared__ int ndone, any_rot;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t gt = int64_t(blockIdx.x) * NT + tid;
+    const int64_t nt = int64_t(gridDim.x) * NT;
+
+    for (int s = 0; s < nsec; ++s) {
+        const SectorDesc sd = P.secs[s];
+        const int64_t qq = int64_t(sd.q) * sd.q;
+        for (int64_t e = gt; e < qq; e += nt) P.rot[sd.rot_off + e] = (e % (sd.q + 1) == 0) ? T(1) : T(0);
+    }
+    if (tid == 0) {
+        ndone = 0;
+        istart[0] = 0;
+    }
+    __syncthreads();
+    for (int s = tid; s < nsec; s += NT) {
+        const int q = P.secs[s].q;
+        done[s] = (q < 2) ? 1 : 0;
+        sweep[s] = 0;
+        istart[s + 1] = bj_items(q, B);
+        if (done[s]) atomicAdd(&ndone, 1);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int carry = 0;
+        for (int base = 0; base < nsec; base += 32) {
+            const int i = base + lane;
+            int v = i < nsec ? istart[i + 1] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            if (i < nsec) istart[i + 1] = v + carry;
+            carry += __shfl_sync(0xffffffffu, v, 31);
+        }
+    }
+    __syncthreads();
+    const int total = istart[nsec];
+    grid.sync();
+
+    for (int64_t step = 0; step < P.max_steps; ++step) {
+        if (ndone >= nsec) break;
+        for (int item = blockIdx.x; item < total; item += gridDim.x) {
+            int lo = 0, hi = nsec - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (istart[mid] <= item)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const int s = lo;
+            if (done[s]) continue;
+            const SectorDesc sd = P.secs[s];
+            const int p = sd.p, q = sd.q;
+            const int nb = (q + B - 1) / B, nbp = nb + (nb & 1);
+            const int k = int(step % (nbp - 1));
+            int a, b;
+            rr_pair(nbp, k, item - istart[s], a, b);
+            if (a > b) {
+                const int t = a;
+                a = b;
+                b = t;
+            }
+            const bool has_b = b < nb;  // otherwise b is the phantom block
+            if (!has_b && k != 0) continue;
+            const int na = min(B, q - a * B), nbc = has_b ? min(B, q - b * B) : 0;
+            auto valid = [&](int j) { return j < B ? j < na : (j - B) < nbc; };
+            auto column = [&](int j) { return j < B ? a * B + j : b * B + (j - B); };
+            T *W = P.work + sd.w_off;
+            T *V = P.rot + sd.rot_off;
+
+            for (int j = warp; j < NP; j += B) {
+                if (!valid(j)) continue;
+                const T *src = W + int64_t(column(j)) * p;
+                for (int r = lane; r < p; r += 32) cols[j * PP + r] = ldcg(src + r);
+            }
+            for (int e = tid; e < NP * NP; e += NT) Qs[e] = (e % (NP + 1) == 0) ? T(1) : T(0);
+            if (tid == 0) any_rot = 0;
+            __syncthreads();
+            bool rotated_any = false;
+            T x[R], y[R], sn, tau;
+            if (k == 0) {
+                // intra-block pairs: round-robin over the B columns of each block
+                const int half = warp / (B / 2), slot = warp % (B / 2);
+                for (int round = 0; round < B - 1; ++round) {
+                    int u, v;
+                    rr_pair(B, round, slot, u, v);
+                    u += half * B;
+                    v += half * B;
+                    if (valid(u) && valid(v)) {
+                        bj_load(x, cols + u * PP, p, lane);
+                        bj_load(y, cols + v * PP, p, lane);
+                        if (bj_rotate(x, y, p, sn, tau)) {
+                            bj_store(x, cols + u * PP, p, lane);
+                            bj_store(y, cols + v * PP, p, lane);
+                            if (lane < NP) {
+                                T qu = Qs[u * NP + lane], qv = Qs[v * NP + lane];
+                                rot_apply(qu, qv, sn, tau);
+                                Qs[u * NP + lane] = qu;
+                                Qs[v * NP + lane] = qv;
+                            }
+                            rotated_any = true;
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            if (has_b) {
+                // inter-block pairs: warp k keeps I_k, the J columns move through shared memory
+                const bool mine = valid(warp);
+                T qx = T(0);
+                if (mine) {
+                    bj_load(x, cols + warp * PP, p, lane);
+                    if (lane < NP) qx = Qs[warp * NP + lane];
+                }
+                bool mine_rot = false;
+                for (int round = 0; round < B; ++round) {
+                    const int j = B + (warp + round) % B;
+                    if (mine && valid(j)) {
+                        bj_load(y, cols + j * PP, p, lane);
+                        if (bj_rotate(x, y, p, sn, tau)) {
+                            bj_store(y, cols + j * PP, p, lane);
+                            if (lane < NP) {
+                                T qy = Qs[j * NP + lane];
+                                rot_apply(qx, qy, sn, tau);
+                                Qs[j * NP + lane] = qy;
+                            }
+                            mine_rot = true;
+                        }
+                    }
+                    __syncthreads();
+                }
+                if (mine_rot) {
+                    bj_store(x, cols + warp * PP, p, lane);
+                    if (lane < NP) Qs[warp * NP + lane] = qx;
+                    rotated_any = true;
+                }
+            }
+            if (rotated_any && lane == 0) any_rot = 1;
+            __syncthreads();
+            if (any_rot) {
+                for (int j = warp; j < NP; j += B) {
+                    if (!valid(j)) continue;
+                    T *dst = W + int64_t(column(j)) * p;
+                    for (int r = lane; r < p; r += 32) dst[r] = cols[j * PP + r];
+                }
+                for (int r = tid; r < q; r += NT) {
+                    T vr[NP];
+#pragma unroll
+                    for (int j = 0; j < NP; ++j) vr[j] = valid(j) ? ldcg(V + int64_t(column(j)) * q + r) : T(0);
+#pragma unroll 4
+                    for (int jp = 0; jp < NP; ++jp) {
+                        if (!valid(jp)) continue;
+                        T acc = 0;
+#pragma unroll
+                        for (int j = 0; j < NP; ++j) acc = fma(vr[j], Qs[jp * NP + j], acc);
+                        V[int64_t(column(jp)) * q + r] = acc;
+                    }
+                }
+                if (tid == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
+            }
+            __syncthreads();
+        }
+        grid.sync();
+        for (int s = tid; s < nsec; s += NT) {
+            if (done[s]) continue;
+            const int nb = (P.secs[s].q + B - 1) / B;
+            const int nbp = nb + (nb & 1);
+            if ((step + 1) % (nbp - 1) == 0) {
+                const int sw = sweep[s];
+                const bool rot = ((volatile int *)P.rotated)[int64_t(s) * P.max_sweeps + sw] != 0;
+                sweep[s] = sw + 1;
+                if (!rot || sw + 1 >= P.max_sweeps) {
+                    done[s] = 1;
+                    atomicAdd(&ndone, 1);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0)
+        for (int s = tid; s < nsec; s += NT) P.sweeps[s] = sweep[s];
 }
 
 // One CTA per sector: column norms, ordering, normalisation, completion.
@@ -427,12 +724,95 @@ void jacobi_launch(const JacobiParams<T> &P, size_t smem, cudaStream_t stream) {
     count_launch();
 }
 
+constexpr int BJ_MAX_SECTORS = 1024;  // per-CTA sector tables of the block kernel
+
+template <class T, int B, int R>
+void bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, cudaStream_t stream) {
+    const size_t smem = size_t(2 * B) * (32 * R + 2 * B) * sizeof(T) + size_t(3 * P.nsec + 1) * sizeof(int);
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        cuda_check(cudaFuncSetAttribute(k_bjacobi<T, B, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024),
+                   "block Jacobi smem attribute");
+    }
+    int occ = 0;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bjacobi<T, B, R>, 32 * B, smem), "occupancy");
+    if (occ < 1) fail(ERR_RUNTIME, "the block Jacobi kernel cannot be resident on an SM");
+    BJacobiParams<T> Pc = P;
+    Pc.max_steps = int64_t(P.max_sweeps) * std::max(1, max_block_steps) + 1;
+    void *args[] = {&Pc};
+    dim3 grid(nsm * std::min(occ, 2)), block(32 * B);
+    cuda_check(cudaLaunchCooperativeKernel((void *)k_bjacobi<T, B, R>, grid, block, args, smem, stream),
+               "cooperative block Jacobi launch");
+    count_launch();
+}
+
+// Block kernel for columns up to 2048 (FP32) / 1536 (FP64) elements and up to
+// 1024 sectors; returns false when the scalar kernel has to run instead.
+template <class T>
+bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int max_p, cudaStream_t stream) {
+    if (P.nsec > BJ_MAX_SECTORS) return false;
+    const int max_qp = max_steps_per_sweep + 1;  // the widest sector's even column count
+    auto steps = [&](int B) {
+        const int nb = (max_qp + B - 1) / B;
+        return nb + (nb & 1) - 1;
+    };
+    if constexpr (sizeof(T) == 4) {
+        if (max_p <= 4 * 32)
+            bjacobi_launch<T, 16, 4>(P, steps(16), stream);
+        else if (max_p <= 8 * 32)
+            bjacobi_launch<T, 16, 8>(P, steps(16), stream);
+        else if (max_p <= 16 * 32)
+            bjacobi_launch<T, 16, 16>(P, steps(16), stream);
+        else if (max_p <= 24 * 32)
+            bjacobi_launch<T, 16, 24>(P, steps(16), stream);
+        else if (max_p <= 32 * 32)
+            bjacobi_launch<T, 16, 32>(P, steps(16), stream);
+        else if (max_p <= 48 * 32)
+            bjacobi_launch<T, 8, 48>(P, steps(8), stream);
+        else if (max_p <= 64 * 32)
+            bjacobi_launch<T, 8, 64>(P, steps(8), stream);
+        else
+            return false;
+    } else {
+        if (max_p <= 4 * 32)
+            bjacobi_launch<T, 8, 4>(P, steps(8), stream);
+        else if (max_p <= 8 * 32)
+            bjacobi_launch<T, 8, 8>(P, steps(8), stream);
+        else if (max_p <= 16 * 32)
+            bjacobi_launch<T, 8, 16>(P, steps(8), stream);
+        else if (max_p <= 24 * 32)
+            bjacobi_launch<T, 8, 24>(P, steps(8), stream);
+        else if (max_p <= 32 * 32)
+            bjacobi_launch<T, 8, 32>(P, steps(8), stream);
+        else if (max_p <= 48 * 32)
+            bjacobi_launch<T, 8, 48>(P, steps(8), stream);
+        else
+            return false;
+    }
+    return true;
+}
+
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
                  int max_sweeps, int *sweeps_out, int *flags, int max_p, cudaStream_t stream) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
+    if (jacobi_variant() != 1) {
+        BJacobiParams<T> B;
+        B.work = work;
+        B.rot = rot;
+        B.secs = sec;
+        B.nsec = nsec;
+        B.max_sweeps = max_sweeps;
+        B.max_steps = 0;
+        B.sweeps = sweeps_out;
+        B.rotated = flags;
+        if (bjacobi_dispatch(B, max_steps_per_sweep, max_p, stream)) return;
+    }
     JacobiParams<T> P;
     P.work = work;
     P.rot = rot;

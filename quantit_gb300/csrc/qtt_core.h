@@ -293,6 +293,10 @@ enum GemmMode : int {
 };
 void set_gemm_mode(int mode);
 int gemm_mode();
+// Sector-SVD Jacobi kernel: 0 = block-cyclic where it fits (default), 1 = scalar
+// (one column pair per warp and grid step).
+void set_jacobi_variant(int v);
+int jacobi_variant();
 // Non-zero when a tensor-core kernel gave up on a bounded wait since the last
 // check (synchronises the device; read and cleared).
 int tc_error_check();

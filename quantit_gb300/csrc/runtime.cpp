@@ -1,6 +1,7 @@
 // Runtime support: per-thread stream context, stream-ordered device memory, the
 // pinned staging ring for planning tables, kernel timing statistics, and the
 // btensor construction / validation helpers.
+#include <atomic>
 #include <mutex>
 #include <numeric>
 #include <sstream>
@@ -178,6 +179,15 @@ void set_gemm_mode(int m) {
     g_gemm_mode = m;
 }
 int gemm_mode() { return g_gemm_mode; }
+
+namespace {
+std::atomic<int> g_jacobi_variant{0};
+}
+void set_jacobi_variant(int v) {
+    if (v < 0 || v > 1) fail(ERR_INVALID_ARGUMENT, "unknown Jacobi kernel variant");
+    g_jacobi_variant = v;
+}
+int jacobi_variant() { return g_jacobi_variant; }
 
 // ---------------------------------------------------------------- btensor helpers
 std::string check_tensor(const BT &t) {
