@@ -60,9 +60,8 @@ __device__ __forceinline__ void rot_apply(T &x, T &y, T s, T tau) {
 
 // Hestenes rotation for column norms al, be and inner product ga: s and tau.
 template <class T>
-__device__ __forceinline__ void rot_params(T al, T be, T ga, T &s, T &tau) {
+__device__ __forceinline__ void rot_params(T al, T be, T ga, T &s, T &tau, T &t) {
     const T zeta = (be - al) / (T(2) * ga);
-    T t;
     if (fabs(zeta) > T(1e18))
         t = T(0.5) / zeta;
     else
@@ -70,6 +69,11 @@ __device__ __forceinline__ void rot_params(T al, T be, T ga, T &s, T &tau) {
     const T c = T(1) / sqrt(T(1) + t * t);
     s = c * t;
     tau = s / (T(1) + c);
+}
+template <class T>
+__device__ __forceinline__ void rot_params(T al, T be, T ga, T &s, T &tau) {
+    T t;
+    rot_params(al, be, ga, s, tau, t);
 }
 
 // Round-robin (circle method) pairing of qp (even) players at round k in [0, qp-1):
@@ -352,56 +356,131 @@ __device__ __forceinline__ int bj_items(int q, int B) {
     return (nb + (nb & 1)) / 2;
 }
 
+// 16-byte shared-memory chunks: lane l holds elements (32 i + l) * V + c of a
+// column, V = 16 / sizeof(T); slots are zero-padded to PP, so no bounds checks.
 template <class T, int R>
-__device__ __forceinline__ void bj_load(T (&x)[R], const T *slot, int p, int lane) {
+__device__ __forceinline__ void bj_load(T (&x)[R], const T *slot, int lane) {
+    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-    for (int i = 0; i < R; ++i) {
-        const int r = lane + 32 * i;
-        x[i] = r < p ? slot[r] : T(0);
+        for (int i = 0; i < R / 4; ++i) {
+            const float4 v = reinterpret_cast<const float4 *>(slot)[32 * i + lane];
+            x[4 * i] = v.x;
+            x[4 * i + 1] = v.y;
+            x[4 * i + 2] = v.z;
+            x[4 * i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i) {
+            const double2 v = reinterpret_cast<const double2 *>(slot)[32 * i + lane];
+            x[2 * i] = v.x;
+            x[2 * i + 1] = v.y;
+        }
     }
 }
 
 template <class T, int R>
-__device__ __forceinline__ void bj_store(const T (&x)[R], T *slot, int p, int lane) {
+__device__ __forceinline__ void bj_store(const T (&x)[R], T *slot, int lane) {
+    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-    for (int i = 0; i < R; ++i) {
-        const int r = lane + 32 * i;
-        if (r < p) slot[r] = x[i];
+        for (int i = 0; i < R / 4; ++i)
+            reinterpret_cast<float4 *>(slot)[32 * i + lane] = make_float4(x[4 * i], x[4 * i + 1], x[4 * i + 2], x[4 * i + 3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i)
+            reinterpret_cast<double2 *>(slot)[32 * i + lane] = make_double2(x[2 * i], x[2 * i + 1]);
     }
 }
 
-// Hestenes rotation of two register-resident columns (same test and formulas as
-// rotate_pair).  Returns whether a rotation was applied, with its s and tau.
 template <class T, int R>
-__device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], int p, T &sn, T &tau) {
-    T al = 0, be = 0, ga = 0;
+__device__ __forceinline__ T bj_dot(const T (&x)[R], const T (&y)[R]) {
+    T a = 0;
 #pragma unroll
-    for (int i = 0; i < R; ++i) {
-        al = fma(x[i], x[i], al);
-        be = fma(y[i], y[i], be);
-        ga = fma(x[i], y[i], ga);
+    for (int i = 0; i < R; ++i) a = fma(x[i], y[i], a);
+    return wsum(a);
+}
+
+// Rotation parameters from the multi-function unit (FP32 only).  t need not be
+// the exact optimum (a near-optimal angle leaves |ga'| ~ 1e-7 |ga|, far under the
+// acceptance threshold); s = t / h and tau = t / (1 + h) with h = sqrt(1 + t^2)
+// define an orthogonal transformation up to O(s^2 * ulp), so approximate
+// reciprocals and square roots cost no accuracy but ~4x less latency than the
+// IEEE-rounded divisions and square roots on the critical path of every round.
+__device__ __forceinline__ void bj_params_fast(float al, float be, float ga, float &sn, float &tau, float &t) {
+    const float zeta = __fdividef(be - al, 2.0f * ga);
+    const float az = fabsf(zeta);
+    if (az > 1e18f) {
+        t = 0.5f / zeta;
+    } else {
+        const float w = fmaf(zeta, zeta, 1.0f);
+        t = copysignf(__fdividef(1.0f, az + w * rsqrtf(w)), zeta);
     }
-    al = wsum(al);
-    be = wsum(be);
-    ga = wsum(ga);
-    if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
-    rot_params(al, be, ga, sn, tau);
+    const float w2 = fmaf(t, t, 1.0f);
+    const float rh = rsqrtf(w2);
+    sn = t * rh;
+    tau = __fdividef(t, 1.0f + w2 * rh);
+}
+
+// Hestenes rotation of two register-resident columns with tracked squared norms
+// al, be: only the inner product is formed; after the rotation the norms follow
+// from al' = al - t ga, be' = be + t ga (t = tan theta), and are recomputed from
+// the columns when that update cancels (norm drops below 1/16).  Same acceptance
+// test and rotation as rotate_pair (tol = Eps<T>::tol(p), hoisted by the caller).
+template <class T, int R>
+__device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T &sn, T &tau) {
+    const T ga = bj_dot(x, y);
+    if (ga == T(0)) return false;
+    T t;
+    if constexpr (sizeof(T) == 4) {
+        if (fabsf(ga) * rsqrtf(al) * rsqrtf(be) <= tol) return false;
+        bj_params_fast(al, be, ga, sn, tau, t);
+    } else {
+        if (fabs(ga) <= tol * sqrt(al * be)) return false;
+        rot_params(al, be, ga, sn, tau, t);
+    }
 #pragma unroll
     for (int i = 0; i < R; ++i) rot_apply(x[i], y[i], sn, tau);
+    const T a2 = al - t * ga, b2 = be + t * ga;
+    al = (a2 > al * T(0.0625)) ? a2 : bj_dot(x, x);
+    be = (b2 > be * T(0.0625)) ? b2 : bj_dot(y, y);
     return true;
+}
+
+template <class T, int NP>
+__device__ __forceinline__ T bj_qdot(const T (&vr)[NP], const T *qcol) {
+    T acc = 0;
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int j = 0; j < NP / 4; ++j) {
+            const float4 qv = reinterpret_cast<const float4 *>(qcol)[j];
+            acc = fma(vr[4 * j], qv.x, acc);
+            acc = fma(vr[4 * j + 1], qv.y, acc);
+            acc = fma(vr[4 * j + 2], qv.z, acc);
+            acc = fma(vr[4 * j + 3], qv.w, acc);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < NP / 2; ++j) {
+            const double2 qv = reinterpret_cast<const double2 *>(qcol)[j];
+            acc = fma(vr[2 * j], qv.x, acc);
+            acc = fma(vr[2 * j + 1], qv.y, acc);
+        }
+    }
+    return acc;
 }
 
 template <class T, int B, int R>
 __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
     constexpr int NP = 2 * B;   // columns (players) of a block pair
-    constexpr int PP = 32 * R;  // shared-memory slot per column
+    constexpr int PP = 32 * R;  // shared-memory slot per column (zero-padded)
     constexpr int NT = 32 * B;
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char bsh[];
     T *cols = reinterpret_cast<T *>(bsh);  // NP slots of PP
     T *Qs = cols + NP * PP;                // NP x NP, column-major
+    T *nrm = Qs + NP * NP;                 // NP squared column norms
     const int nsec = P.nsec;
-    int *done = reinterpret_cast<int *>(Qs + NP * NP);
+    int *done = reinterpret_cast<int *>(nrm + NP);
     int *sweep = done + nsec;
     int *istart = sweep + nsec;  // nsec + 1 prefix sums of block pairs per step
     __shared__ int ndone, any_rot;
@@ -475,11 +554,19 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             auto column = [&](int j) { return j < B ? a * B + j : b * B + (j - B); };
             T *W = P.work + sd.w_off;
             T *V = P.rot + sd.rot_off;
+            const T tol = Eps<T>::tol(p);
 
             for (int j = warp; j < NP; j += B) {
                 if (!valid(j)) continue;
                 const T *src = W + int64_t(column(j)) * p;
-                for (int r = lane; r < p; r += 32) cols[j * PP + r] = ldcg(src + r);
+                T acc = 0;
+                for (int r = lane; r < PP; r += 32) {
+                    const T v = r < p ? ldcg(src + r) : T(0);
+                    acc = fma(v, v, acc);
+                    cols[j * PP + r] = v;
+                }
+                acc = wsum(acc);
+                if (lane == 0) nrm[j] = acc;
             }
             for (int e = tid; e < NP * NP; e += NT) Qs[e] = (e % (NP + 1) == 0) ? T(1) : T(0);
             if (tid == 0) any_rot = 0;
@@ -495,16 +582,21 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     u += half * B;
                     v += half * B;
                     if (valid(u) && valid(v)) {
-                        bj_load(x, cols + u * PP, p, lane);
-                        bj_load(y, cols + v * PP, p, lane);
-                        if (bj_rotate(x, y, p, sn, tau)) {
-                            bj_store(x, cols + u * PP, p, lane);
-                            bj_store(y, cols + v * PP, p, lane);
+                        bj_load(x, cols + u * PP, lane);
+                        bj_load(y, cols + v * PP, lane);
+                        T al = nrm[u], be = nrm[v];
+                        if (bj_rotate(x, y, al, be, tol, sn, tau)) {
+                            bj_store(x, cols + u * PP, lane);
+                            bj_store(y, cols + v * PP, lane);
                             if (lane < NP) {
                                 T qu = Qs[u * NP + lane], qv = Qs[v * NP + lane];
                                 rot_apply(qu, qv, sn, tau);
                                 Qs[u * NP + lane] = qu;
                                 Qs[v * NP + lane] = qv;
+                            }
+                            if (lane == 0) {
+                                nrm[u] = al;
+                                nrm[v] = be;
                             }
                             rotated_any = true;
                         }
@@ -515,30 +607,33 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             if (has_b) {
                 // inter-block pairs: warp k keeps I_k, the J columns move through shared memory
                 const bool mine = valid(warp);
-                T qx = T(0);
+                T qx = T(0), al = T(0);
                 if (mine) {
-                    bj_load(x, cols + warp * PP, p, lane);
+                    bj_load(x, cols + warp * PP, lane);
                     if (lane < NP) qx = Qs[warp * NP + lane];
+                    al = nrm[warp];
                 }
                 bool mine_rot = false;
                 for (int round = 0; round < B; ++round) {
                     const int j = B + (warp + round) % B;
                     if (mine && valid(j)) {
-                        bj_load(y, cols + j * PP, p, lane);
-                        if (bj_rotate(x, y, p, sn, tau)) {
-                            bj_store(y, cols + j * PP, p, lane);
+                        bj_load(y, cols + j * PP, lane);
+                        T be = nrm[j];
+                        if (bj_rotate(x, y, al, be, tol, sn, tau)) {
+                            bj_store(y, cols + j * PP, lane);
                             if (lane < NP) {
                                 T qy = Qs[j * NP + lane];
                                 rot_apply(qx, qy, sn, tau);
                                 Qs[j * NP + lane] = qy;
                             }
+                            if (lane == 0) nrm[j] = be;
                             mine_rot = true;
                         }
                     }
                     __syncthreads();
                 }
                 if (mine_rot) {
-                    bj_store(x, cols + warp * PP, p, lane);
+                    bj_store(x, cols + warp * PP, lane);
                     if (lane < NP) Qs[warp * NP + lane] = qx;
                     rotated_any = true;
                 }
@@ -555,13 +650,10 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     T vr[NP];
 #pragma unroll
                     for (int j = 0; j < NP; ++j) vr[j] = valid(j) ? ldcg(V + int64_t(column(j)) * q + r) : T(0);
-#pragma unroll 4
+#pragma unroll 2
                     for (int jp = 0; jp < NP; ++jp) {
                         if (!valid(jp)) continue;
-                        T acc = 0;
-#pragma unroll
-                        for (int j = 0; j < NP; ++j) acc = fma(vr[j], Qs[jp * NP + j], acc);
-                        V[int64_t(column(jp)) * q + r] = acc;
+                        V[int64_t(column(jp)) * q + r] = bj_qdot<T, NP>(vr, Qs + jp * NP);
                     }
                 }
                 if (tid == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
@@ -728,7 +820,7 @@ constexpr int BJ_MAX_SECTORS = 1024;  // per-CTA sector tables of the block kern
 
 template <class T, int B, int R>
 void bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, cudaStream_t stream) {
-    const size_t smem = size_t(2 * B) * (32 * R + 2 * B) * sizeof(T) + size_t(3 * P.nsec + 1) * sizeof(int);
+    const size_t smem = size_t(2 * B) * (32 * R + 2 * B + 1) * sizeof(T) + size_t(3 * P.nsec + 1) * sizeof(int);
     static int nsm = 0;
     if (!nsm) {
         int dev = 0;
