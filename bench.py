@@ -48,6 +48,16 @@ def parse():
     p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving"],
+                   help="dmrg: the D=2048 sweep line (with a short serving section); serving: the full "
+                        "Poisson request stream of XXZ solves (L in 16..128, D in 32..512)")
+    p.add_argument("--serving-requests", type=int, default=16)
+    p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate (requests/s)")
+    p.add_argument("--serving-slots", type=int, default=8)
+    p.add_argument("--serving-fp64-every", type=int, default=4,
+                   help="serial FP64 baseline on every k-th request of the stream")
+    p.add_argument("--serving-fp64-budget", type=float, default=300.0,
+                   help="stop the serial FP64 sample once this many seconds are spent")
     p.add_argument("--jacobi", default="block", choices=["block", "scalar"],
                    help="sector-SVD Jacobi kernel (block-cyclic where it fits, or scalar)")
     return p.parse_args()
@@ -263,6 +273,48 @@ def e2e_sweep(q, mpo, mps, args):
     return {"value": dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "E": E}
 
 
+SERVING_REDUCED = dict(lengths=(16, 32, 64), bonds=(32, 64, 128, 256))
+SERVING_FULL = dict(lengths=(16, 32, 64, 128), bonds=(32, 64, 128, 256, 512))
+
+
+def serving_section(q, args, full):
+    """Continuous-batching solves of a seeded Poisson stream of XXZ requests (mixed
+    precision, converged to 1e-8 relative energy), and serial plain-FP64 solves of
+    every k-th request of the same stream as the baseline."""
+    from quantit_gb300 import serving
+    dist = SERVING_FULL if full else SERVING_REDUCED
+    reqs = serving.poisson_requests(args.serving_requests, rate=args.serving_rate, seed=0, **dist)
+    eng = serving.ServingEngine(slots=args.serving_slots, gemm=args.mode if args.mode != "f64" else "tf32x3",
+                                convergence=1e-8, max_sweeps=40)
+    res = eng.run(reqs, realtime=True)
+    mk = max(r.done for r in res) - min(r.arrival for r in res)
+    out = serving.summarize([r.latency for r in res], mk, len(res))
+    out.update({"requests": len(reqs), "rate_per_s": args.serving_rate, "slots": args.serving_slots,
+                "distribution": {"L": list(dist["lengths"]), "D": list(dist["bonds"]), "delta": [0.0, 2.0]},
+                "convergence": 1e-8, "gemm": "tf32x3", "peak_concurrency": eng.peak_concurrency,
+                "memory_budget_bytes": eng.memory_budget, "peak_admitted_bytes": eng.peak_memory,
+                "errors": sum(1 for r in res if r.error),
+                "mean_service_s": float(np.mean([r.service for r in res])),
+                "latency": "completion minus arrival (queueing included)"})
+    sample, st = [], []
+    t0 = time.perf_counter()
+    for r in reqs[::max(1, args.serving_fp64_every)]:
+        if sample and time.perf_counter() - t0 > args.serving_fp64_budget:
+            break
+        st += serving.serial_solve_times([r], gemm="f64", convergence=1e-8, max_sweeps=40)
+        sample.append(r)
+    svc = [x[0] for x in st]
+    mixed = {r.rid: r for r in res}
+    dE = [abs(mixed[r.rid].energy - x[1]) / r.L for r, x in zip(sample, st)]
+    out["serial_fp64"] = {"sample": len(sample), "of_every": args.serving_fp64_every,
+                          "sampled": [[r.L, r.D] for r in sample],
+                          "solves_per_s": len(sample) / sum(svc), "mean_service_s": float(np.mean(svc)),
+                          "max_dE_per_site_vs_mixed": float(max(dE)),
+                          "note": "one solve at a time on the GPU, plain FP64"}
+    out["throughput_vs_serial_fp64"] = out["solves_per_s"] / out["serial_fp64"]["solves_per_s"]
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -284,6 +336,19 @@ def main():
     import quantit_gb300 as q
     q.ensure_init(local)
     q.set_jacobi_kernel(args.jacobi)
+    if args.workload == "serving":
+        sv = serving_section(q, args, full=True)
+        if rank == 0:
+            print(json.dumps({"metric": "solves/s (XXZ ground states, Poisson arrivals) at p99 latency",
+                              "value": sv["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": 1,
+                              "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                              "dtype": "tf32x3+f32svd+f64", "data": "synthetic",
+                              "config": {"workload": "serving: Poisson stream of XXZ chain ground-state solves",
+                                         "parallelism": "replicas only" if world > 1 else "single GPU"},
+                              "serving": sv}))
+        if world > 1:
+            dist.destroy_process_group()
+        return
     mpo, mps0 = build_state(q, args.L, args.D, seed=rank)
     _, _, mps1 = run_sweeps(q, mpo, mps0, args.warmup, args.mode, args.D)
     q.stats.reset()
@@ -340,6 +405,11 @@ def main():
                                               f"x {s.factor:.1f} size-weighted bonds per sweep"}
         except Exception as e:  # reported, never hidden
             line["cpu_baseline"] = {"error": repr(e)}
+    if rank == 0 and args.serving_requests > 0:
+        try:
+            line["serving"] = serving_section(q, args, full=False)
+        except Exception as e:  # reported, never hidden
+            line["serving"] = {"error": repr(e)}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

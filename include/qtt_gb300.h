@@ -66,6 +66,9 @@ int qtt_synchronize(void);
 /* Block-GEMM precision for the calling process (QTT_GEMM_*). */
 int qtt_set_gemm_mode(int mode);
 int qtt_get_gemm_mode(void);
+/* Free and total bytes of the calling thread's device (no reference counterpart;
+ * the serving loop admits solves against it). */
+int qtt_device_memory(int64_t *free_bytes, int64_t *total_bytes);
 /* Sector-SVD kernel (no reference counterpart; a tuning and testing switch):
  * 0 = block-cyclic Jacobi wherever the sector shapes fit it (default),
  * 1 = scalar Jacobi (one column pair per warp and grid step) everywhere. */
@@ -160,8 +163,10 @@ typedef struct {
     int64_t minimum_bond;          /* default 4 */
     int64_t maximum_iterations;    /* sweeps (default 1000) */
     int32_t gemm_mode;             /* QTT_GEMM_* for the matvecs and environment updates */
-    int32_t final_energy_fp64;     /* mixed gemm_mode: return the FP64 <psi|H|psi>/<psi|psi> of the
-                                      final state instead of the last Ritz value (default 1) */
+    int32_t final_energy_fp64;     /* mixed gemm_mode: use the FP64 <psi|H|psi>/<psi|psi> of the state
+                                      instead of the last Ritz value -- after every sweep for the
+                                      convergence test and the log when convergence_criterion > 0,
+                                      and for the returned energy (default 1) */
 } qtt_dmrg_options;
 /* dmrg_options defaults (include/dmrg_options.h:15-58) */
 void qtt_dmrg_options_default(qtt_dmrg_options *opt);

@@ -19,7 +19,8 @@ class dmrg_options:
         self.minimum_bond = min_bond
         self.maximum_iterations = maximum_iterations
         self.gemm = gemm
-        # mixed precision: return the FP64 <psi|H|psi>/<psi|psi> of the final state
+        # mixed precision: the FP64 <psi|H|psi>/<psi|psi> of the state replaces the Ritz
+        # value after every sweep (convergence test, log) and as the returned energy
         self.final_energy_fp64 = final_energy_fp64
 
     def _c(self):

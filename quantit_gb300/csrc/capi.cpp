@@ -84,6 +84,15 @@ int qtt_set_gemm_mode(int mode) {
     return guarded([&] { qtt::set_gemm_mode(mode); });
 }
 int qtt_get_gemm_mode(void) { return qtt::gemm_mode(); }
+int qtt_device_memory(int64_t *free_bytes, int64_t *total_bytes) {
+    return guarded([&] {
+        if (!free_bytes || !total_bytes) qtt::fail(qtt::ERR_INVALID_ARGUMENT, "null output pointer");
+        size_t f = 0, t = 0;
+        qtt::cuda_check(cudaMemGetInfo(&f, &t), "cudaMemGetInfo");
+        *free_bytes = int64_t(f);
+        *total_bytes = int64_t(t);
+    });
+}
 int qtt_set_jacobi_kernel(int which) {
     return guarded([&] { qtt::set_jacobi_variant(which); });
 }

@@ -236,7 +236,7 @@ namespace {
 // Split every block of t (legs permuted by perm; the first nrow legs form the
 // rows, the rest the contracted K) into hi / lo TF32 arrays in matrix form.
 void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std::vector<int64_t> &offs, BufPtr &hi,
-                   BufPtr &lo) {
+                   BufPtr &lo, unsigned long long *amax) {
     const int r = t.rank;
     const int64_t nb = t.nblocks();
     offs.assign(nb, 0);
@@ -277,8 +277,9 @@ void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std:
     cuda_check(cudaMemsetAsync(lo->p, 0, bytes, ctx().stream), "cudaMemsetAsync(split)");
     auto chunks = make_chunks(lens);
     StatScope sc(ST_PACK, 16.0 * double(std::accumulate(lens.begin(), lens.end(), int64_t(0))));
+    launch_amax(static_cast<const double *>(t.data()), t.nnz, amax);
     launch_split_tf32(static_cast<const double *>(t.data()), static_cast<float *>(hi->p), static_cast<float *>(lo->p),
-                      upload_vec(ents), upload_vec(chunks), int64_t(chunks.size()));
+                      upload_vec(ents), upload_vec(chunks), int64_t(chunks.size()), amax);
 }
 }  // namespace
 
@@ -291,15 +292,18 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
     const int mode = gemm_mode();
     const bool tc = mode != GEMM_F64;
     // operand buffers
-    BufPtr pa, pb, ahi, alo, bhi, blo;
+    BufPtr pa, pb, ahi, alo, bhi, blo, amax;
     std::vector<int64_t> offa, offb;
     const double *Ap = static_cast<const double *>(A.data());
     const double *Bp = static_cast<const double *>(B.data());
     const std::vector<int64_t> *oa = &A.boff, *ob = &B.boff;
     int a_t = 0, b_t = 0;
     if (tc) {
-        split_operand(A, P.p1, int(P.freeA.size()), offa, ahi, alo);
-        split_operand(B, P.p2p, int(P.freeB.size()), offb, bhi, blo);
+        amax = dev_alloc(2 * sizeof(unsigned long long));
+        cuda_check(cudaMemsetAsync(amax->p, 0, 2 * sizeof(unsigned long long), ctx().stream), "cudaMemsetAsync(amax)");
+        auto *am = static_cast<unsigned long long *>(amax->p);
+        split_operand(A, P.p1, int(P.freeA.size()), offa, ahi, alo, am);
+        split_operand(B, P.p2p, int(P.freeB.size()), offb, bhi, blo, am + 1);
         oa = &offa;
         ob = &offb;
     } else {
@@ -376,6 +380,8 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
         g.Alo = static_cast<const float *>(alo->p);
         g.Bhi = static_cast<const float *>(bhi->p);
         g.Blo = static_cast<const float *>(blo->p);
+        g.amax_a = static_cast<const unsigned long long *>(amax->p);
+        g.amax_b = g.amax_a + 1;
         g.C = static_cast<double *>(out.data());
         g.Cadd = add ? static_cast<const double *>(add->data()) : nullptr;
         g.pairs = dpairs;

@@ -148,12 +148,7 @@ double sum_all(const BT &t) {
 double mps_energy(const std::vector<BT> &mpo, const std::vector<BT> &mps, double *norm2) {
     const int64_t L = int64_t(mpo.size());
     if (L < 1 || int64_t(mps.size()) != L) fail(ERR_INVALID_ARGUMENT, "MPO and MPS need the same length");
-    const int saved = gemm_mode();
-    set_gemm_mode(GEMM_F64);
-    struct G {
-        int m;
-        ~G() { set_gemm_mode(m); }
-    } guard{saved};
+    ScopedGemmMode guard(GEMM_F64);
     BT env = trivial_edge(mps[0], 0, mpo[0], 0);
     for (int64_t i = 0; i < L; ++i) env = compute_left_env(mpo[i], mps[i], env);
     const double e = sum_all(env);
@@ -168,12 +163,7 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
             void *user) {
     const int64_t L = int64_t(mpo.size());
     if (L < 2 || int64_t(mps.size()) != L) fail(ERR_INVALID_ARGUMENT, "MPO and MPS need the same length >= 2");
-    const int saved_mode = gemm_mode();
-    set_gemm_mode(opt.gemm_mode);
-    struct ModeGuard {
-        int m;
-        ~ModeGuard() { set_gemm_mode(m); }
-    } guard{saved_mode};
+    ScopedGemmMode guard(opt.gemm_mode);
     // compute_2sitesHamil (dmrg.cpp:504-515)
     std::vector<BT> h2(L - 1);
     for (int64_t i = 0; i < L - 1; ++i) h2[i] = compute_2sites_hamil(mpo[i], mpo[i + 1]);
@@ -186,6 +176,8 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
     for (int64_t i = L - 1; i > oc; --i) env[i + 1] = compute_right_env(mpo[i], mps[i], env[i + 2]);
     // dmrg_impl (dmrg.cpp:219-273)
     double E0 = 100000.0;
+    const bool fp64_energy = opt.gemm_mode != GEMM_F64 && opt.final_energy_fp64;
+    bool last_fp64 = false;  // E0 is the FP64 energy of the current state
     int64_t init_pos = oc;
     const int64_t nh = L - 1;
     const int64_t n_step = nh - 1 + (nh == 1);
@@ -234,6 +226,14 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
         cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
         tc_error_raise();
         double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        // mixed path: the Ritz values carry FP32-level noise (~1e-7 relative), under which
+        // a tight relative criterion never fires; test the FP64 energy of the sweep's state
+        last_fp64 = fp64_energy && opt.convergence_criterion > 0.0;
+        if (last_fp64) {
+            double n2 = 1.0;
+            const double e = mps_energy(mpo, mps, &n2);
+            E = e / n2;
+        }
         if (log) log(user, it, E, secs);
         double prev = E0;
         E0 = E;
@@ -245,7 +245,7 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
                                   std::to_string(oc) + ". original oc: " + std::to_string(init_pos));
     }
     oc_io = oc;
-    if (opt.gemm_mode != GEMM_F64 && opt.final_energy_fp64) {
+    if (fp64_energy && !last_fp64) {
         // the mixed path's Ritz values carry the FP32-level noise of its block
         // GEMMs; the variational energy of its final state, reduced in FP64, does not
         double n2 = 1.0;

@@ -26,6 +26,7 @@
 // a device word that the host checks, still waits (bounded) for its MMAs and
 // frees its TMEM before returning.
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.h"
 #include "qtt_core.h"
@@ -87,9 +88,17 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
     return r;
 }
 
-// FP64 -> FP32 (round to nearest, ties away) with integer operations only.
+// Exponent of an operand's max |x| (the scale 2^-shift brings it to [1, 2));
+// zero, infinite or NaN maxima leave the operand unscaled.
+__device__ __forceinline__ int amax_shift(unsigned long long bits) {
+    const int e = int((bits >> 52) & 0x7FF);
+    if (e == 0x7FF || bits == 0) return 0;
+    return (e == 0 ? 1 : e) - 1023;
+}
+
+// FP64 * 2^-shift -> FP32 (round to nearest, ties away) with integer operations only.
 // Magnitudes below the FP32 normal range flush to zero.
-__device__ __forceinline__ float f64_to_f32_int(double x) {
+__device__ __forceinline__ float f64_to_f32_int(double x, int shift) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
     const uint32_t sign = uint32_t(b >> 63) << 31;
     const int e = int((b >> 52) & 0x7FF);
@@ -100,7 +109,7 @@ __device__ __forceinline__ float f64_to_f32_int(double x) {
     } else if (e == 0x7FF) {
         f = 0x7F800000u | (m ? 0x400000u : 0u);
     } else {
-        const int fe = e - 1023 + 127;
+        const int fe = e - 1023 + 127 - shift;
         if (fe <= 0) {
             f = 0;
         } else if (fe >= 255) {
@@ -114,26 +123,50 @@ __device__ __forceinline__ float f64_to_f32_int(double x) {
     return __uint_as_float(sign | f);
 }
 
-// FP32 -> FP64 (exact) with integer operations only; FP32 subnormals flush to zero.
-__device__ __forceinline__ double f32_to_f64_int(float f) {
+// FP32 * 2^shift -> FP64 (exact unless the result leaves the FP64 normal range,
+// where it flushes to zero or saturates to infinity) with integer operations only;
+// FP32 subnormals flush to zero.
+__device__ __forceinline__ double f32_to_f64_int(float f, int shift) {
     const uint32_t b = __float_as_uint(f);
     const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
     const uint32_t e = (b >> 23) & 0xFF, m = b & 0x7FFFFF;
     unsigned long long d;
-    if (e == 0)
+    if (e == 0) {
         d = sign;
-    else if (e == 0xFF)
+    } else if (e == 0xFF) {
         d = sign | 0x7FF0000000000000ull | ((unsigned long long)m << 29);
-    else
-        d = sign | ((unsigned long long)(e - 127 + 1023) << 52) | ((unsigned long long)m << 29);
+    } else {
+        const int de = int(e) - 127 + 1023 + shift;
+        if (de <= 0)
+            d = sign;
+        else if (de >= 0x7FF)
+            d = sign | 0x7FF0000000000000ull;
+        else
+            d = sign | ((unsigned long long)de << 52) | ((unsigned long long)m << 29);
+    }
     return __longlong_as_double(static_cast<long long>(d));
 }
 
+__global__ void k_amax(const double *__restrict__ x, int64_t n, unsigned long long *amax) {
+    unsigned long long m = 0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const unsigned long long v = static_cast<unsigned long long>(__double_as_longlong(x[i])) & 0x7FFFFFFFFFFFFFFFull;
+        m = v > m ? v : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long u = __shfl_xor_sync(0xffffffffu, m, o);
+        m = u > m ? u : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(amax, m);
+}
+
 __global__ void k_split_tf32(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo,
-                             const SplitEntry *__restrict__ ents, const Chunk *__restrict__ chunks) {
+                             const SplitEntry *__restrict__ ents, const Chunk *__restrict__ chunks,
+                             const unsigned long long *__restrict__ amax) {
     const Chunk ch = chunks[blockIdx.x];
     const SplitEntry &e = ents[ch.seg];
     const int r = e.rank;
+    const int shift = amax_shift(*amax);
     for (int i = threadIdx.x; i < ch.len; i += blockDim.x) {
         const int64_t lin = ch.start + i;
         int64_t rem = lin, so = e.src_off;
@@ -143,7 +176,7 @@ __global__ void k_split_tf32(const double *__restrict__ src, float *__restrict__
             so += (rem - q * n) * e.stride[d];
             rem = q;
         }
-        const float xf = f64_to_f32_int(src[so]);
+        const float xf = f64_to_f32_int(src[so], shift);
         const uint32_t h = to_tf32(xf);
         const uint32_t l = to_tf32(xf - __uint_as_float(h));
         const int64_t row = lin / e.K, k = lin - row * e.K;
@@ -277,6 +310,7 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
 
     // epilogue: warp w reads TMEM lanes 32*(w%4).., columns 64*(w/4) .. +63
     const int quarter = warp & 3, half = warp >> 2;
+    const int shift = amax_shift(*g.amax_a) + amax_shift(*g.amax_b);
     const int row = quarter * 32 + lane;
     const int gm = t.m0 + row;
     const bool have_acc = nchunk > 0 && !abort_flag;
@@ -309,7 +343,7 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
                 const int gn = t.n0 + col0 + j;
                 if (gn < o.N) {
                     const int64_t idx = int64_t(gm) * o.N + gn;
-                    double val = f32_to_f64_int(__uint_as_float(v[j]));
+                    double val = f32_to_f64_int(__uint_as_float(v[j]), shift);
                     if (!plain) {
                         val *= g.alpha;
                         if (o.add_off >= 0) val += g.beta * g.Cadd[o.add_off + idx];
@@ -327,15 +361,15 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
     }
 }
 
-std::atomic<bool> g_tc_used{false};  // a tensor-core launch happened since the last error check
-
+// the calling thread's error word (one per stream context, so concurrent solves
+// on different threads see only their own kernels' status)
 int *err_word() {
-    static int *p = nullptr;
-    if (!p) {
-        cuda_check(cudaMalloc(&p, sizeof(int)), "cudaMalloc(error word)");
-        cuda_check(cudaMemset(p, 0, sizeof(int)), "cudaMemset(error word)");
+    Ctx &c = ctx();
+    if (!c.tc_err) {
+        cuda_check(cudaMalloc(&c.tc_err, sizeof(int)), "cudaMalloc(error word)");
+        cuda_check(cudaMemset(c.tc_err, 0, sizeof(int)), "cudaMemset(error word)");
     }
-    return p;
+    return c.tc_err;
 }
 
 }  // namespace
@@ -344,35 +378,44 @@ int gemm_tile_m(int) { return TBM; }
 int gemm_tile_n(int) { return TBN; }
 
 void launch_split_tf32(const double *src, float *hi, float *lo, const SplitEntry *e, const Chunk *chunks,
-                       int64_t nchunks) {
+                       int64_t nchunks, const unsigned long long *amax) {
     if (nchunks <= 0) return;
-    k_split_tf32<<<unsigned(nchunks), 256, 0, ctx().stream>>>(src, hi, lo, e, chunks);
+    k_split_tf32<<<unsigned(nchunks), 256, 0, ctx().stream>>>(src, hi, lo, e, chunks, amax);
     count_launch();
     cuda_check(cudaGetLastError(), "split kernel launch");
+}
+
+void launch_amax(const double *x, int64_t n, unsigned long long *amax) {
+    if (n <= 0) return;
+    const int64_t blocks = std::min<int64_t>((n + 2047) / 2048, 4 * 152);
+    k_amax<<<unsigned(blocks), 256, 0, ctx().stream>>>(x, n, amax);
+    count_launch();
+    cuda_check(cudaGetLastError(), "amax kernel launch");
 }
 
 void launch_gemm_tc(const TcArgs &a, int mode) {
     if (mode != GEMM_TF32X3) fail(ERR_INVALID_ARGUMENT, "this tensor-core GEMM precision mode is not built");
     if (a.ntiles <= 0) return;
-    static bool attr = false;
-    if (!attr) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
                    "tcgen05 GEMM smem attribute");
-        attr = true;
-    }
+    });
     k_gemm_tf32x3<<<a.ntiles, TTHREADS, SMEM_BYTES, ctx().stream>>>(a, err_word());
     count_launch();
-    g_tc_used = true;
+    ctx().tc_used = true;
     cuda_check(cudaGetLastError(), "tcgen05 GEMM launch");
 }
 
 // Non-zero when a tensor-core kernel hit a bounded wait (read and cleared; synchronises).
 int tc_error_check() {
-    if (!g_tc_used.exchange(false)) return 0;
+    Ctx &c = ctx();
+    if (!c.tc_used) return 0;
+    c.tc_used = false;
     int h = 0;
-    cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
-    cuda_check(cudaMemcpy(&h, err_word(), sizeof(int), cudaMemcpyDeviceToHost), "read error word");
-    if (h) cuda_check(cudaMemset(err_word(), 0, sizeof(int)), "clear error word");
+    cuda_check(cudaMemcpyAsync(&h, err_word(), sizeof(int), cudaMemcpyDeviceToHost, c.stream), "read error word");
+    cuda_check(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+    if (h) cuda_check(cudaMemsetAsync(err_word(), 0, sizeof(int), c.stream), "clear error word");
     return h;
 }
 

@@ -13,6 +13,8 @@
 // Every loop is bounded: at most max_sweeps sweeps per sector.
 #include <cooperative_groups.h>
 
+#include <mutex>
+
 #include "kernels.h"
 #include "qtt_core.h"
 
@@ -793,24 +795,34 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
     }
 }
 
-template <class T, int R>
-void jacobi_launch(const JacobiParams<T> &P, size_t smem, cudaStream_t stream) {
+int sm_count() {
+    static std::once_flag once;
     static int nsm = 0;
-    static int per_sm = 0;
-    if (!nsm) {
+    std::call_once(once, [] {
         int dev = 0;
         cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
         cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    });
+    return nsm;
+}
+
+// Cooperative grids are sized to the work (pairs or block pairs per step), not to
+// the whole GPU, so that small decompositions on concurrent streams overlap.
+template <class T, int R>
+void jacobi_launch(const JacobiParams<T> &P, size_t smem, int64_t pairs_bound, cudaStream_t stream) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_jacobi<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
                    "Jacobi smem attribute");
-    }
+    });
+    const int nsm = sm_count();
     int occ = 0;
     cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_jacobi<T, R>, JJ, smem), "occupancy");
     if (occ < 1) fail(ERR_RUNTIME, "the Jacobi kernel cannot be resident on an SM");
-    per_sm = std::min(occ, 4);
+    const int64_t want = std::max<int64_t>(1, (pairs_bound + JJ / 32 - 1) / (JJ / 32));
     JacobiParams<T> Pc = P;
     void *args[] = {&Pc};
-    dim3 grid(nsm * per_sm), block(JJ);
+    dim3 grid(unsigned(std::min<int64_t>(int64_t(nsm) * std::min(occ, 4), want))), block(JJ);
     cuda_check(cudaLaunchCooperativeKernel((void *)k_jacobi<T, R>, grid, block, args, smem, stream),
                "cooperative Jacobi launch");
     count_launch();
@@ -819,23 +831,24 @@ void jacobi_launch(const JacobiParams<T> &P, size_t smem, cudaStream_t stream) {
 constexpr int BJ_MAX_SECTORS = 1024;  // per-CTA sector tables of the block kernel
 
 template <class T, int B, int R>
-void bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, cudaStream_t stream) {
+void bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_q, cudaStream_t stream) {
     const size_t smem = size_t(2 * B) * (32 * R + 2 * B + 1) * sizeof(T) + size_t(3 * P.nsec + 1) * sizeof(int);
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    static std::once_flag attr;
+    std::call_once(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_bjacobi<T, B, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024),
                    "block Jacobi smem attribute");
-    }
+    });
+    const int nsm = sm_count();
     int occ = 0;
     cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bjacobi<T, B, R>, 32 * B, smem), "occupancy");
     if (occ < 1) fail(ERR_RUNTIME, "the block Jacobi kernel cannot be resident on an SM");
     BJacobiParams<T> Pc = P;
     Pc.max_steps = int64_t(P.max_sweeps) * std::max(1, max_block_steps) + 1;
     void *args[] = {&Pc};
-    dim3 grid(nsm * std::min(occ, 2)), block(32 * B);
+    // block pairs per step: sum over sectors of ceil(ceil(q / B) / 2) <= sum_q / (2B) + nsec
+    const int64_t items = sum_q / (2 * B) + P.nsec;
+    dim3 grid(unsigned(std::min<int64_t>(int64_t(nsm) * std::min(occ, 2), std::max<int64_t>(1, items)))),
+        block(32 * B);
     cuda_check(cudaLaunchCooperativeKernel((void *)k_bjacobi<T, B, R>, grid, block, args, smem, stream),
                "cooperative block Jacobi launch");
     count_launch();
@@ -844,7 +857,8 @@ void bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, cudaStream_t
 // Block kernel for columns up to 2048 (FP32) / 1536 (FP64) elements and up to
 // 1024 sectors; returns false when the scalar kernel has to run instead.
 template <class T>
-bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int max_p, cudaStream_t stream) {
+bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int max_p, int64_t sum_q,
+                      cudaStream_t stream) {
     if (P.nsec > BJ_MAX_SECTORS) return false;
     const int max_qp = max_steps_per_sweep + 1;  // the widest sector's even column count
     auto steps = [&](int B) {
@@ -853,34 +867,34 @@ bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int ma
     };
     if constexpr (sizeof(T) == 4) {
         if (max_p <= 4 * 32)
-            bjacobi_launch<T, 16, 4>(P, steps(16), stream);
+            bjacobi_launch<T, 16, 4>(P, steps(16), sum_q, stream);
         else if (max_p <= 8 * 32)
-            bjacobi_launch<T, 16, 8>(P, steps(16), stream);
+            bjacobi_launch<T, 16, 8>(P, steps(16), sum_q, stream);
         else if (max_p <= 16 * 32)
-            bjacobi_launch<T, 16, 16>(P, steps(16), stream);
+            bjacobi_launch<T, 16, 16>(P, steps(16), sum_q, stream);
         else if (max_p <= 24 * 32)
-            bjacobi_launch<T, 16, 24>(P, steps(16), stream);
+            bjacobi_launch<T, 16, 24>(P, steps(16), sum_q, stream);
         else if (max_p <= 32 * 32)
-            bjacobi_launch<T, 16, 32>(P, steps(16), stream);
+            bjacobi_launch<T, 16, 32>(P, steps(16), sum_q, stream);
         else if (max_p <= 48 * 32)
-            bjacobi_launch<T, 8, 48>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
         else if (max_p <= 64 * 32)
-            bjacobi_launch<T, 8, 64>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 64>(P, steps(8), sum_q, stream);
         else
             return false;
     } else {
         if (max_p <= 4 * 32)
-            bjacobi_launch<T, 8, 4>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 4>(P, steps(8), sum_q, stream);
         else if (max_p <= 8 * 32)
-            bjacobi_launch<T, 8, 8>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 8>(P, steps(8), sum_q, stream);
         else if (max_p <= 16 * 32)
-            bjacobi_launch<T, 8, 16>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 16>(P, steps(8), sum_q, stream);
         else if (max_p <= 24 * 32)
-            bjacobi_launch<T, 8, 24>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 24>(P, steps(8), sum_q, stream);
         else if (max_p <= 32 * 32)
-            bjacobi_launch<T, 8, 32>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 32>(P, steps(8), sum_q, stream);
         else if (max_p <= 48 * 32)
-            bjacobi_launch<T, 8, 48>(P, steps(8), stream);
+            bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
         else
             return false;
     }
@@ -889,7 +903,7 @@ bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int ma
 
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
-                 int max_sweeps, int *sweeps_out, int *flags, int max_p, cudaStream_t stream) {
+                 int max_sweeps, int *sweeps_out, int *flags, int max_p, int64_t sum_q, cudaStream_t stream) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
@@ -903,7 +917,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
         B.max_steps = 0;
         B.sweeps = sweeps_out;
         B.rotated = flags;
-        if (bjacobi_dispatch(B, max_steps_per_sweep, max_p, stream)) return;
+        if (bjacobi_dispatch(B, max_steps_per_sweep, max_p, sum_q, stream)) return;
     }
     JacobiParams<T> P;
     P.work = work;
@@ -915,29 +929,29 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     P.max_steps = int64_t(max_sweeps) * std::max(1, max_steps_per_sweep) + 1;
     P.sweeps = sweeps_out;
     P.rotated = flags;
+    const int64_t pairs = (sum_q + nsec) / 2 + nsec;  // pairs per step, an upper bound
     // registers per lane: the longest column over the sectors decides
     if (max_p <= 4 * 32)
-        jacobi_launch<T, 4>(P, smem, stream);
+        jacobi_launch<T, 4>(P, smem, pairs, stream);
     else if (max_p <= 8 * 32)
-        jacobi_launch<T, 8>(P, smem, stream);
+        jacobi_launch<T, 8>(P, smem, pairs, stream);
     else if (max_p <= 16 * 32)
-        jacobi_launch<T, 16>(P, smem, stream);
+        jacobi_launch<T, 16>(P, smem, pairs, stream);
     else if (max_p <= 32 * 32)
-        jacobi_launch<T, 32>(P, smem, stream);
+        jacobi_launch<T, 32>(P, smem, pairs, stream);
     else
-        jacobi_launch<T, 0>(P, smem, stream);
+        jacobi_launch<T, 0>(P, smem, pairs, stream);
 }
 
 template <class T>
 void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
                  int max_q, double *scratch, cudaStream_t stream) {
     size_t smem = size_t(max_q) * (sizeof(double) + sizeof(int)) + 16;
-    static bool attr = false;
-    if (!attr) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_finish<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
                    "finish smem attribute");
-        attr = true;
-    }
+    });
     if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the SVD finishing kernel");
     k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch);
     count_launch();
@@ -968,20 +982,21 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p) {
+                      int max_p, int64_t sum_q) {
     if (nsec <= 0) return;
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
-                    max_sweeps, sweeps_out, flags, max_p, stream);
+                    max_sweeps, sweeps_out, flags, max_p, sum_q, stream);
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
-                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, stream);
+                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, stream);
 }
 
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p) {
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
+                   int64_t sum_q) {
     launch_jacobi_on(ctx().stream, work, rot, sec, slot_start, nsec, max_steps_per_sweep, max_sweeps, sweeps_out, flags,
-                     f32, max_p);
+                     f32, max_p, sum_q);
 }
 
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,

@@ -74,11 +74,18 @@ struct SplitEntry {
     int64_t dims[8];
     int64_t stride[8];
 };
+// amax: the bit pattern of max |x| over the operand (launch_amax); every element is
+// scaled by the exact power of two 2^-ilogb(amax) before the split, so operands of any
+// magnitude use the FP32 range, and the GEMM epilogue undoes the two scales exactly.
 void launch_split_tf32(const double *src, float *hi, float *lo, const SplitEntry *e, const Chunk *chunks,
-                       int64_t nchunks);
+                       int64_t nchunks, const unsigned long long *amax);
+// *amax (zeroed by the caller) <- max(*amax, bits of |x|) over n doubles (bit order =
+// value order for non-negative doubles, so the maximum is exact and deterministic).
+void launch_amax(const double *x, int64_t n, unsigned long long *amax);
 // A pair's a_off / b_off index the split arrays; A rows = M, B rows = N, K4 = (K + 3) & ~3.
 struct TcArgs {
     const float *Ahi, *Alo, *Bhi, *Blo;
+    const unsigned long long *amax_a, *amax_b;  // operand scales (see launch_split_tf32)
     double *C;
     const double *Cadd;
     const GemmPair *pairs;
@@ -154,8 +161,10 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 // ((q + q%2)/2); max_steps_per_sweep = max over sectors of (q + q%2 - 1).
 // sweeps_out[s] receives the number of sweeps sector s used; flags holds
 // nsec*max_sweeps ints of scratch.
+// sum_q: the sectors' total column count (sizes the cooperative grid to the work).
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
-                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p);
+                   int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
+                   int64_t sum_q);
 // Column norms, sort (descending for svd, ascending eigenvalues for eigh),
 // normalisation and completion of null columns; writes U (m x k), V (n x k)
 // column-major and s (k) per sector in FP64, k = min(m, n).  max_q: largest q;
@@ -165,7 +174,7 @@ void launch_finish(const void *work, const void *rot, double *U, double *V, doub
 // The same two launches on an explicit stream (no library context involved).
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p);
+                      int max_p, int64_t sum_q);
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
                       const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32);
 // Segment = one output block (rows x k row-major at dst_off) from a column-major

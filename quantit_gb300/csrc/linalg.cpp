@@ -143,7 +143,7 @@ struct LastSweeps {
     int n = 0;
 };
 LastSweeps &last_sweeps() {
-    static LastSweeps l;
+    thread_local LastSweeps l;  // per host thread, like its stream
     return l;
 }
 
@@ -262,7 +262,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     }
     {
         StatScope sc(ST_SVD, 0.0);
-        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p);
+        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot);
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
                       static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32);
     }

@@ -113,7 +113,7 @@ void svd_dense_noalloc(const double *a, int64_t m, int64_t n, double *u, double 
     k_na_pack<<<64, 256, 0, st>>>(a, int(m), int(n), W, d.trans);
     qtt::cuda_check(cudaGetLastError(), "no-alloc pack launch");
     // the Jacobi kernel initialises the rotation; the launcher clears the flags
-    qtt::launch_jacobi_on(st, W, rot, desc, slots, 1, std::max(1, qp - 1), kMaxSweeps, sweeps, flags, 0, d.p);
+    qtt::launch_jacobi_on(st, W, rot, desc, slots, 1, std::max(1, qp - 1), kMaxSweeps, sweeps, flags, 0, d.p, d.q);
     qtt::launch_finish_on(st, W, rot, Uc, Vc, s, desc, 1, d.q, scr, 0);
     k_na_rowmajor<<<64, 256, 0, st>>>(Uc, int(m), d.q, u);
     k_na_rowmajor<<<64, 256, 0, st>>>(Vc, int(n), d.q, v);

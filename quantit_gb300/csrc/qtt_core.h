@@ -141,6 +141,9 @@ struct Ctx {
     cudaEvent_t half_done[2] = {nullptr, nullptr};
     int cur_half = 0;
     bool half_used[2] = {false, false};
+    // error word of this thread's tensor-core launches (bounded waits that expired)
+    int *tc_err = nullptr;
+    bool tc_used = false;
 };
 Ctx &ctx();
 void set_stream(cudaStream_t s);
@@ -291,8 +294,15 @@ enum GemmMode : int {
     GEMM_TF32X3 = 1,     // split TF32 on tcgen05, FP32 accumulation, 3 products
     GEMM_BF16X3 = 2,     // split BF16 on tcgen05, FP32 accumulation, 3 products
 };
-void set_gemm_mode(int mode);
-int gemm_mode();
+void set_gemm_mode(int mode);  // process-wide default
+int gemm_mode();               // the calling thread's override, else the default
+// Per-thread override for the duration of a call (a DMRG solve runs its own
+// precision without touching other threads' solves).
+struct ScopedGemmMode {
+    int saved;
+    explicit ScopedGemmMode(int mode);
+    ~ScopedGemmMode();
+};
 // Sector-SVD Jacobi kernel: 0 = block-cyclic where it fits (default), 1 = scalar
 // (one column pair per warp and grid step).
 void set_jacobi_variant(int v);

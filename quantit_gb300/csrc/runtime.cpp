@@ -172,13 +172,19 @@ void count_launch(int n) { g_launches += n; }
 
 // ---------------------------------------------------------------- gemm mode
 namespace {
-int g_gemm_mode = GEMM_F64;
+std::atomic<int> g_gemm_mode{GEMM_F64};
+thread_local int tl_gemm_mode = -1;  // -1: no override on this thread
 }
 void set_gemm_mode(int m) {
     if (m < GEMM_F64 || m > GEMM_BF16X3) fail(ERR_INVALID_ARGUMENT, "unknown GEMM precision mode");
     g_gemm_mode = m;
 }
-int gemm_mode() { return g_gemm_mode; }
+int gemm_mode() { return tl_gemm_mode >= 0 ? tl_gemm_mode : g_gemm_mode.load(); }
+ScopedGemmMode::ScopedGemmMode(int mode) : saved(tl_gemm_mode) {
+    if (mode < GEMM_F64 || mode > GEMM_BF16X3) fail(ERR_INVALID_ARGUMENT, "unknown GEMM precision mode");
+    tl_gemm_mode = mode;
+}
+ScopedGemmMode::~ScopedGemmMode() { tl_gemm_mode = saved; }
 
 namespace {
 std::atomic<int> g_jacobi_variant{0};

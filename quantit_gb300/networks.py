@@ -180,7 +180,11 @@ def bond_sectors(L, D, phys_q, target):
 
 
 def random_bmps(L, D, phys_q=(1, -1), target=0, seed=0):
-    """Seeded random normalised U(1) MPS (orthogonality centre 0 after move_oc)."""
+    """Seeded random U(1) MPS in the manner of random_bMPS (sources/MPT.cpp:424-460):
+    N(0,1) blocks, every site tensor scaled to unit Frobenius norm, no canonical
+    form (so the environments of a long chain shrink geometrically; the FP64 path
+    and the mixed path's power-of-two operand scaling both handle that).  The
+    orthogonality centre is recorded as the last site, where a sweep starts."""
     rng = np.random.default_rng(seed)
     bonds = bond_sectors(L, D, list(phys_q), target)
     _, psecs = _group_by_charge(list(phys_q))

@@ -1,0 +1,34 @@
+"""Serving loop on the GPU (pytest -m gpu): every request solved inside the mix of
+concurrently admitted solves gives the same energy as the same request solved
+alone, and the mixed-precision energies agree with FP64 solves."""
+import numpy as np
+import pytest
+
+from quantit_gb300 import serving
+
+pytestmark = pytest.mark.gpu
+
+REQS = [serving.SolveRequest(i, L, delta, D, seed=100 + i)
+        for i, (L, delta, D) in enumerate([(8, 0.3, 8), (12, 1.0, 16), (16, 1.7, 16), (10, 0.0, 12),
+                                           (14, 0.8, 32), (12, 2.0, 8), (16, 1.2, 24), (8, 1.5, 16)])]
+
+
+def test_results_same_alone_and_in_the_mix():
+    alone = serving.serial_solve_times(REQS, gemm="tf32x3", convergence=1e-8, max_sweeps=30)
+    eng = serving.ServingEngine(slots=4, gemm="tf32x3", convergence=1e-8, max_sweeps=30)
+    mixed = eng.run(REQS, realtime=False)
+    assert eng.peak_concurrency >= 2
+    for (t, E, sw), r in zip(alone, mixed):
+        assert r.error is None, r.error
+        # per-stream kernels are deterministic: the mix changes timing, not arithmetic
+        assert r.energy == pytest.approx(E, rel=1e-12, abs=1e-12), (r.rid, r.energy, E)
+        assert r.sweeps == sw
+
+
+def test_mixed_serving_energies_match_fp64_solves():
+    sub = REQS[:4]
+    ref = serving.serial_solve_times(sub, gemm="f64", convergence=1e-10, max_sweeps=30)
+    eng = serving.ServingEngine(slots=4, gemm="tf32x3", convergence=1e-8, max_sweeps=30)
+    res = eng.run(sub, realtime=False)
+    for (t, E, sw), r in zip(ref, res):
+        assert abs(r.energy - E) / r.L < 1e-7, (r.rid, r.energy, E)

@@ -96,3 +96,32 @@ def test_mixed_dmrg_energy_close_to_fp64():
             if mode == "tf32x3":
                 assert res[mode] == pytest.approx(e / n2, rel=1e-14)
         assert abs(res["tf32x3"] - res["f64"]) / L < 1e-8, (L, D, res)
+
+
+@pytest.mark.parametrize("scale_a, scale_b", [(1e-60, 1.0), (1e-30, 1e-30), (1e45, 1e-40), (3e-200, 2e150)])
+def test_tc_gemm_operand_magnitudes(tf32x3, scale_a, scale_b):
+    # operands far outside the FP32 range: each is scaled by an exact power of two
+    # before the split and the product is scaled back in the epilogue
+    rng = np.random.default_rng(24)
+    A, B, dA, dB = _contractible_pair(rng, (0,), 3, 3, 1)
+    while not A.blocks or not B.blocks:
+        A, B, dA, dB = _contractible_pair(rng, (0,), 3, 3, 1)
+    A = o.scale(A, scale_a)
+    B = o.scale(B, scale_b)
+    _check(to_device(A).tensordot(to_device(B), (dA, dB)), o.tensordot(A, B, dA, dB))
+
+
+def test_mixed_dmrg_from_noncanonical_state():
+    """random_bmps (like random_bMPS) is not in canonical form: the left environments
+    of L=32 shrink to ~1e-60 before the first sweep.  The mixed path must still
+    converge to the FP64 path's energy."""
+    L, D = 32, 48
+    mpo = q.networks.xxz(L, 1.0)
+    out = {}
+    for gemm in ("f64", "tf32x3"):
+        mps = q.networks.random_bmps(L, D, seed=5)
+        opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=1e-9, max_bond=D, min_bond=1,
+                                         maximum_iterations=20, gemm=gemm, final_energy_fp64=True)
+        out[gemm] = q.algorithms.dmrg(mpo, mps, opts)
+    assert np.isfinite(out["tf32x3"])
+    assert abs(out["tf32x3"] - out["f64"]) / L < 1e-7, out
