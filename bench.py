@@ -248,7 +248,7 @@ def roofline(kind, st, P, mode, peaks_cache):
             import torch
             peaks_cache[key] = matmul_peak_tflops(torch.float32 if fp32 else torch.float64)
         ach = st["work"] / sec / 1e12
-        return dict(base, bound="latency (one grid barrier per Jacobi step)" if kind == "svd" else "fp64",
+        return dict(base, bound="latency (grid barrier per block-Jacobi step, CTA barrier per round)" if kind == "svd" else "fp64",
                     achieved=ach, peak=peaks_cache[key], unit="TFLOP/s", frac=ach / peaks_cache[key],
                     peak_source=f"cuBLAS {'SGEMM' if fp32 else 'DGEMM'} measured in this run")
     ach = st["work"] / sec / 1e9
