@@ -43,8 +43,11 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--L", type=int, default=32)
-    p.add_argument("--D", type=int, default=2048)
+    p.add_argument("--model", default="heisenberg", choices=["heisenberg", "hubbard"],
+                   help="heisenberg: spin-1/2 chain, U(1) (defaults L=32, D=2048); hubbard: Fermi-Hubbard "
+                        "U=8 at half filling, U(1)xU(1) (defaults L=64, D=1024)")
+    p.add_argument("--L", type=int, default=None)
+    p.add_argument("--D", type=int, default=None)
     p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -117,9 +120,13 @@ def peaks():
         return {}
 
 
-def build_state(q, L, D, seed=0):
-    mpo = q.networks.heisenberg(L)
-    mps = q.networks.random_bmps(L, D, seed=seed)
+def build_state(q, L, D, seed=0, model="heisenberg"):
+    if model == "hubbard":
+        mpo = q.networks.hubbard(L, 8.0)
+        mps = q.networks.random_bmps(L, D, q.networks.HUBBARD_PHYS, (L, 0), seed=seed, mods=(0, 0))
+    else:
+        mpo = q.networks.heisenberg(L)
+        mps = q.networks.random_bmps(L, D, seed=seed)
     mps.move_oc(0)
     mps.normalize_center()
     return mpo, mps
@@ -318,14 +325,29 @@ def serving_section(q, args, full):
 def main():
     args = parse()
     rank, world, local = dist_env()
-    cfg = {"workload": f"Heisenberg chain L={args.L}, two-site DMRG sweep at D={args.D}, U(1) Sz=0",
-           "L": args.L, "D": args.D, "model": "spin-1/2 Heisenberg open chain (J=1 AFM)",
+    hub = args.model == "hubbard"
+    if args.L is None:
+        args.L = 64 if hub else 32
+    if args.D is None:
+        args.D = 1024 if hub else 2048
+    if hub:
+        cfg = {"workload": f"Fermi-Hubbard chain L={args.L}, U=8, half filling, two-site DMRG sweep at D={args.D}, "
+                           "U(1)xU(1) (N, 2Sz)", "L": args.L, "D": args.D,
+               "model": "Fermi-Hubbard open chain t=1 U=8 mu=0, N=L, Sz=0"}
+    else:
+        cfg = {"workload": f"Heisenberg chain L={args.L}, two-site DMRG sweep at D={args.D}, U(1) Sz=0",
+               "L": args.L, "D": args.D, "model": "spin-1/2 Heisenberg open chain (J=1 AFM)"}
+    cfg.update({
            "cutoff": 1e-10, "update": "one-step Lanczos (QuantiT two_sites_update)",
            "l2": "working set (MPS + environments) far larger than L2 (129 MB)",
-           "parallelism": "replicas only" if world > 1 else "single GPU"}
+           "parallelism": "replicas only" if world > 1 else "single GPU"})
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(reference_arm(args, cfg)))
+            if hub:
+                print(json.dumps({"impl": "reference", "unavailable": "the CPU sampler restates the Heisenberg "
+                                  "bond update only; the Hubbard model runs on the GPU paths"}))
+            else:
+                print(json.dumps(reference_arm(args, cfg)))
         return
 
     import torch
@@ -349,7 +371,7 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return
-    mpo, mps0 = build_state(q, args.L, args.D, seed=rank)
+    mpo, mps0 = build_state(q, args.L, args.D, seed=rank, model=args.model)
     _, _, mps1 = run_sweeps(q, mpo, mps0, args.warmup, args.mode, args.D)
     q.stats.reset()
     q.stats.enable(True)
@@ -395,7 +417,9 @@ def main():
             "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e}
     if cmp:
         line["vs_fp64"] = cmp
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and hub:
+        line["cpu_baseline"] = None  # the oracle sampler restates the Heisenberg bond update only
+    elif rank == 0 and not args.no_cpu_baseline:
         try:
             s = CpuSampler(args.L, args.D)
             per = [s.bond() for _ in range(2)]
@@ -405,7 +429,7 @@ def main():
                                               f"x {s.factor:.1f} size-weighted bonds per sweep"}
         except Exception as e:  # reported, never hidden
             line["cpu_baseline"] = {"error": repr(e)}
-    if rank == 0 and args.serving_requests > 0:
+    if rank == 0 and args.serving_requests > 0 and not hub:
         try:
             line["serving"] = serving_section(q, args, full=False)
         except Exception as e:  # reported, never hidden

@@ -828,14 +828,18 @@ void jacobi_launch(const JacobiParams<T> &P, size_t smem, int64_t pairs_bound, c
     count_launch();
 }
 
-constexpr int BJ_MAX_SECTORS = 1024;  // per-CTA sector tables of the block kernel
+constexpr size_t BJ_SMEM_MAX = 220 * 1024;  // dynamic shared memory of one block-Jacobi CTA
 
+// false when the columns and the per-CTA sector tables (3 ints per sector) do not
+// fit one CTA's shared memory; the scalar kernel runs instead
 template <class T, int B, int R>
-void bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_q, cudaStream_t stream) {
+bool bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_q, cudaStream_t stream) {
     const size_t smem = size_t(2 * B) * (32 * R + 2 * B + 1) * sizeof(T) + size_t(3 * P.nsec + 1) * sizeof(int);
+    if (smem > BJ_SMEM_MAX) return false;
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cuda_check(cudaFuncSetAttribute(k_bjacobi<T, B, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024),
+        cuda_check(cudaFuncSetAttribute(k_bjacobi<T, B, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(BJ_SMEM_MAX)),
                    "block Jacobi smem attribute");
     });
     const int nsm = sm_count();
@@ -852,14 +856,15 @@ void bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_
     cuda_check(cudaLaunchCooperativeKernel((void *)k_bjacobi<T, B, R>, grid, block, args, smem, stream),
                "cooperative block Jacobi launch");
     count_launch();
+    return true;
 }
 
-// Block kernel for columns up to 2048 (FP32) / 1536 (FP64) elements and up to
-// 1024 sectors; returns false when the scalar kernel has to run instead.
+// Block kernel for columns up to 2048 (FP32) / 1536 (FP64) elements, as many
+// sectors as the shared-memory tables allow; returns false when the scalar kernel
+// has to run instead.
 template <class T>
 bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int max_p, int64_t sum_q,
                       cudaStream_t stream) {
-    if (P.nsec > BJ_MAX_SECTORS) return false;
     const int max_qp = max_steps_per_sweep + 1;  // the widest sector's even column count
     auto steps = [&](int B) {
         const int nb = (max_qp + B - 1) / B;
@@ -867,38 +872,35 @@ bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int ma
     };
     if constexpr (sizeof(T) == 4) {
         if (max_p <= 4 * 32)
-            bjacobi_launch<T, 16, 4>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 4>(P, steps(16), sum_q, stream);
         else if (max_p <= 8 * 32)
-            bjacobi_launch<T, 16, 8>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 8>(P, steps(16), sum_q, stream);
         else if (max_p <= 16 * 32)
-            bjacobi_launch<T, 16, 16>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 16>(P, steps(16), sum_q, stream);
         else if (max_p <= 24 * 32)
-            bjacobi_launch<T, 16, 24>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 24>(P, steps(16), sum_q, stream);
         else if (max_p <= 32 * 32)
-            bjacobi_launch<T, 16, 32>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 32>(P, steps(16), sum_q, stream);
         else if (max_p <= 48 * 32)
-            bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
         else if (max_p <= 64 * 32)
-            bjacobi_launch<T, 8, 64>(P, steps(8), sum_q, stream);
-        else
-            return false;
+            return bjacobi_launch<T, 8, 64>(P, steps(8), sum_q, stream);
+        return false;
     } else {
         if (max_p <= 4 * 32)
-            bjacobi_launch<T, 8, 4>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 4>(P, steps(8), sum_q, stream);
         else if (max_p <= 8 * 32)
-            bjacobi_launch<T, 8, 8>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 8>(P, steps(8), sum_q, stream);
         else if (max_p <= 16 * 32)
-            bjacobi_launch<T, 8, 16>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 16>(P, steps(8), sum_q, stream);
         else if (max_p <= 24 * 32)
-            bjacobi_launch<T, 8, 24>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 24>(P, steps(8), sum_q, stream);
         else if (max_p <= 32 * 32)
-            bjacobi_launch<T, 8, 32>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 32>(P, steps(8), sum_q, stream);
         else if (max_p <= 48 * 32)
-            bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
-        else
-            return false;
+            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
+        return false;
     }
-    return true;
 }
 
 template <class T>

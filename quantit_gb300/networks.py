@@ -17,7 +17,7 @@ import math
 import numpy as np
 
 from . import linalg
-from .conserved import Z
+from .conserved import Z, quantity
 from .tensor import btensor, dot_all, from_blocks
 
 
@@ -58,6 +58,32 @@ class bMPS(list):
         return self
 
 
+class _Charges:
+    """Charge arithmetic on plain tuples for one group (moduli: 0 = U(1), n = Z(n));
+    plain ints are the one-component U(1) case."""
+
+    def __init__(self, mods=(0,)):
+        self.mods = tuple(int(m) for m in mods)
+
+    def norm(self, c):
+        c = (c,) if isinstance(c, (int, np.integer)) else tuple(c)
+        if len(c) != len(self.mods):
+            raise ValueError("charge with the wrong number of components")
+        return tuple((int(v) % m) if m else int(v) for v, m in zip(c, self.mods))
+
+    def add(self, a, b):
+        return self.norm(tuple(x + y for x, y in zip(a, b)))
+
+    def neg(self, a):
+        return self.norm(tuple(-x for x in a))
+
+    def zero(self):
+        return tuple(0 for _ in self.mods)
+
+    def q(self, c):
+        return quantity(c, self.mods)
+
+
 def _group_by_charge(q):
     order = sorted(range(len(q)), key=lambda i: (q[i], i))
     secs = []
@@ -88,40 +114,85 @@ def heisenberg_dense(J=-1.0, delta=1.0):
     return w
 
 
-def dense_mpo_to_bmpo(ws, phys_q):
-    """U(1) block MPO from dense site tensors: bond charges solved from the nonzero
-    elements, equal charges grouped into one section (the layout of bMPO::coalesce)."""
-    bq = [[0] * ws[0].shape[0]]
+def fermions():
+    """(c_up, c_dn, F, id) on the basis {empty, up, down, up+down} (fermions(),
+    sources/operators.cpp:21-39; the down operator carries the on-site sign)."""
+    c_up = np.zeros((4, 4))
+    c_dn = np.zeros((4, 4))
+    c_up[0, 1] = 1.0
+    c_up[2, 3] = 1.0
+    c_dn[0, 2] = 1.0
+    c_dn[1, 3] = -1.0
+    F = np.diag([1.0, -1.0, -1.0, 1.0])
+    return c_up, c_dn, F, np.eye(4)
+
+
+def hubbard_dense(U, mu):
+    """Bulk W[a, s, b, s'] of Hubbard(U, mu, L) (sources/models.cpp:118-148): the
+    6x4x6x4 operator matrix with hopping channels c^dg F, F c and the on-site term
+    U n_up n_dn - mu (n_up + n_dn)."""
+    c_up, c_dn, F, idm = fermions()
+    n_up = c_up.T @ c_up
+    n_dn = c_dn.T @ c_dn
+    w = np.zeros((6, 4, 6, 4))
+    w[0, :, 0, :] = idm
+    w[1, :, 0, :] = c_up
+    w[2, :, 0, :] = c_dn
+    w[3, :, 0, :] = c_up.T
+    w[4, :, 0, :] = c_dn.T
+    w[5, :, 0, :] = U * (n_up @ n_dn) - mu * (n_up + n_dn)
+    w[5, :, 1, :] = c_up.T @ F
+    w[5, :, 2, :] = c_dn.T @ F
+    w[5, :, 3, :] = F @ c_up
+    w[5, :, 4, :] = F @ c_dn
+    w[5, :, 5, :] = idm
+    return w
+
+
+# physical charges (N, 2 Sz) of the Hubbard basis {empty, up, down, up+down}
+HUBBARD_PHYS = [(0, 0), (1, 1), (1, -1), (2, 0)]
+
+
+def dense_mpo_to_bmpo(ws, phys_q, mods=(0,)):
+    """Block MPO from dense site tensors: bond charges solved from the nonzero
+    elements, equal charges grouped into one section (the layout of bMPO::coalesce).
+    Charges are ints (U(1)) or tuples of the group given by ``mods``."""
+    G = _Charges(mods)
+    pq = [G.norm(c) for c in phys_q]
+    bq = [[G.zero()] * ws[0].shape[0]]
     for w in ws:
         qa = bq[-1]
         qb = [None] * w.shape[2]
         for a, s, b, t in zip(*np.nonzero(w)):
-            v = qa[a] + phys_q[s] - phys_q[t]
+            v = G.add(G.add(qa[a], pq[s]), G.neg(pq[t]))
             if qb[b] is None:
                 qb[b] = v
             elif qb[b] != v:
                 raise ValueError("MPO is not charge conserving")
-        bq.append([0 if q is None else q for q in qb])
-    porder, psecs = _group_by_charge(phys_q)
+        bq.append([G.zero() if q is None else q for q in qb])
+    porder, psecs = _group_by_charge(pq)
     out = bMPO()
     for i, w in enumerate(ws):
         lorder, lsecs = _group_by_charge(bq[i])
         rorder, rsecs = _group_by_charge(bq[i + 1])
         wp = w[np.ix_(lorder, porder, rorder, porder)]
-        legs = [[(n, Z(q)) for n, q in lsecs], [(n, Z(q)) for n, q in psecs],
-                [(n, Z(-q)) for n, q in rsecs], [(n, Z(-q)) for n, q in psecs]]
-        sizes = [[n for n, _ in l] for l in legs]
-        charges = [[q.values[0] for _, q in l] for l in legs]
-        offs = [np.concatenate([[0], np.cumsum(s)]).astype(int) for s in sizes]
+        charges = [[q for _, q in lsecs], [q for _, q in psecs], [G.neg(q) for _, q in rsecs],
+                   [G.neg(q) for _, q in psecs]]
+        sizes = [[n for n, _ in l] for l in (lsecs, psecs, rsecs, psecs)]
+        legs = [[(n, G.q(c)) for n, c in zip(sz, ch)] for sz, ch in zip(sizes, charges)]
+        offs = [np.concatenate([[0], np.cumsum(sz)]).astype(int) for sz in sizes]
         blocks = []
-        for idx in itertools.product(*[range(len(s)) for s in sizes]):
+        for idx in itertools.product(*[range(len(sz)) for sz in sizes]):
             sl = tuple(slice(offs[d][j], offs[d][j + 1]) for d, j in enumerate(idx))
             blk = wp[sl]
             if np.any(blk != 0.0):
-                if sum(charges[d][j] for d, j in enumerate(idx)) != 0:
+                tot = G.zero()
+                for d, j in enumerate(idx):
+                    tot = G.add(tot, charges[d][j])
+                if tot != G.zero():
                     raise ValueError("nonzero MPO element outside the selection rule")
                 blocks.append((idx, np.ascontiguousarray(blk)))
-        out.append(from_blocks(legs, Z(0), blocks))
+        out.append(from_blocks(legs, G.q(G.zero()), blocks))
     return out
 
 
@@ -134,6 +205,14 @@ def heisenberg(L, J=-1.0, delta=1.0):
 
 def xxz(L, delta, J=-1.0):
     return heisenberg(L, J=J, delta=delta)
+
+
+def hubbard(L, U, mu=0.0):
+    """Open Fermi-Hubbard chain (Hubbard(U, mu, L, shape), sources/models.cpp:118-172)
+    with U(1)xU(1) charges (N, 2 Sz) on the physical basis {empty, up, down, up+down}."""
+    w = hubbard_dense(U, mu)
+    ws = [w[5:6]] + [w] * (L - 2) + [w[:, :, 0:1]]
+    return dense_mpo_to_bmpo(ws, HUBBARD_PHYS, mods=(0, 0))
 
 
 def cap_sectors(mult, D):
@@ -158,51 +237,61 @@ def cap_sectors(mult, D):
     return {q: m for q, m in sorted(dims.items()) if m > 0}
 
 
-def bond_sectors(L, D, phys_q, target):
+def bond_sectors(L, D, phys_q, target, mods=(0,)):
     """Sector dimensions of every bond: dict partial charge -> dimension."""
-    left = [{0: 1}]
+    G = _Charges(mods)
+    pq = [G.norm(c) for c in phys_q]
+    tg = G.norm(target)
+    left = [{G.zero(): 1}]
     for _ in range(L):
         nxt = {}
         for q, m in left[-1].items():
-            for p in phys_q:
-                nxt[q + p] = nxt.get(q + p, 0) + m
+            for p in pq:
+                k = G.add(q, p)
+                nxt[k] = nxt.get(k, 0) + m
         left.append(nxt)
     bonds = []
     for b in range(L - 1):
         nl, nr = b + 1, L - b - 1
         dims = {}
         for q, m in left[nl].items():
-            mr = left[nr].get(target - q, 0)
+            mr = left[nr].get(G.add(tg, G.neg(q)), 0)
             if mr:
                 dims[q] = min(m, mr)
-        bonds.append(cap_sectors(dims, D))
+        capped = cap_sectors(dims, D)
+        bonds.append(capped if len(mods) > 1 or mods[0] else {k[0]: v for k, v in capped.items()})
     return bonds
 
 
-def random_bmps(L, D, phys_q=(1, -1), target=0, seed=0):
-    """Seeded random U(1) MPS in the manner of random_bMPS (sources/MPT.cpp:424-460):
+def random_bmps(L, D, phys_q=(1, -1), target=0, seed=0, mods=(0,)):
+    """Seeded random MPS in the manner of random_bMPS (sources/MPT.cpp:424-460):
     N(0,1) blocks, every site tensor scaled to unit Frobenius norm, no canonical
     form (so the environments of a long chain shrink geometrically; the FP64 path
     and the mixed path's power-of-two operand scaling both handle that).  The
-    orthogonality centre is recorded as the last site, where a sweep starts."""
+    orthogonality centre is recorded as the last site, where a sweep starts.
+    Charges are ints (U(1)) or tuples of the group given by ``mods``."""
+    G = _Charges(mods)
     rng = np.random.default_rng(seed)
-    bonds = bond_sectors(L, D, list(phys_q), target)
-    _, psecs = _group_by_charge(list(phys_q))
+    bonds = [{G.norm(k): v for k, v in b.items()} for b in bond_sectors(L, D, phys_q, target, mods)]
+    pq = [G.norm(c) for c in phys_q]
+    tg = G.norm(target)
+    _, psecs = _group_by_charge(pq)
+    zero = G.zero()
     mps = bMPS(orthogonality_center=L - 1)
     for i in range(L):
-        lleg = [(1, Z(0))] if i == 0 else [(m, Z(q - target)) for q, m in bonds[i - 1].items()]
-        rleg = [(1, Z(0))] if i == L - 1 else [(m, Z(target - q)) for q, m in bonds[i].items()]
-        legs = [lleg, [(n, Z(q)) for n, q in psecs], rleg]
-        sel = target if i == 0 else 0
+        lq = [zero] if i == 0 else [G.add(q, G.neg(tg)) for q in bonds[i - 1]]
+        lm = [1] if i == 0 else list(bonds[i - 1].values())
+        rq = [zero] if i == L - 1 else [G.add(tg, G.neg(q)) for q in bonds[i]]
+        rm = [1] if i == L - 1 else list(bonds[i].values())
+        sel = tg if i == 0 else zero
+        legs = [[(m, G.q(c)) for m, c in zip(lm, lq)], [(n, G.q(c)) for n, c in psecs],
+                [(m, G.q(c)) for m, c in zip(rm, rq)]]
         blocks = []
-        lq = [q.values[0] for _, q in lleg]
-        pq = [q for _, q in psecs]
-        rq = [q.values[0] for _, q in rleg]
-        for a, s, b in itertools.product(range(len(lleg)), range(len(psecs)), range(len(rleg))):
-            if lq[a] + pq[s] + rq[b] == sel:
-                shp = (lleg[a][0], psecs[s][0], rleg[b][0])
-                blocks.append(((a, s, b), rng.standard_normal(shp)))
+        for a, s_, b in itertools.product(range(len(lq)), range(len(psecs)), range(len(rq))):
+            if G.add(G.add(lq[a], psecs[s_][1]), rq[b]) == sel:
+                shp = (lm[a], psecs[s_][0], rm[b])
+                blocks.append(((a, s_, b), rng.standard_normal(shp)))
         nrm = math.sqrt(sum(float(np.sum(v ** 2)) for _, v in blocks))
         blocks = [(k, v / nrm) for k, v in blocks]
-        mps.append(from_blocks(legs, Z(sel), blocks))
+        mps.append(from_blocks(legs, G.q(sel), blocks))
     return mps
