@@ -138,33 +138,65 @@ ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_
             o.cv.push_back(B.cv[adB[d] + s]);
         }
     }
-    // merge-join (btensor.cpp:1998-2114)
+    // merge-join (btensor.cpp:1998-2114): for every run of A (equal free prefix) and
+    // every run of B, in that nested order, the pairs with equal contracted suffix.
+    // Only the runs of B that share a suffix with the run of A can produce pairs, so
+    // they are found through a sorted (suffix, run) index of B instead of trying
+    // every run pair: the same output block list and pair order, in
+    // O(n log n + pairs) instead of O(runs_A x runs_B).
     Keyed t1 = permuted_sorted(A, p1), t2 = permuted_sorted(B, p2p);
     const int nfa = A.rank - dl, nfb = B.rank - dl;
     auto r1 = runs(t1, nfa, dl == 0), r2 = runs(t2, nfb, dl == 0);
-    for (auto &ra : r1) {
-        for (auto &rb : r2) {
-            size_t ia = ra.first, ib = rb.first;
-            size_t first_pair = P.pair_a.size();
-            while (ia < ra.second && ib < rb.second) {
-                const int64_t *sa = t1.k(ia) + nfa, *sb = t2.k(ib) + nfb;
-                if (idx_less(sa, sb, dl))
-                    ++ia;
-                else if (idx_less(sb, sa, dl))
-                    ++ib;
-                else {
-                    P.pair_a.push_back(t1.id[ia]);
-                    P.pair_b.push_back(t2.id[ib]);
-                    ++ia;
-                    ++ib;
-                }
+    auto join = [&](const std::pair<size_t, size_t> &ra, const std::pair<size_t, size_t> &rb) {
+        size_t ia = ra.first, ib = rb.first;
+        size_t first_pair = P.pair_a.size();
+        while (ia < ra.second && ib < rb.second) {
+            const int64_t *sa = t1.k(ia) + nfa, *sb = t2.k(ib) + nfb;
+            if (idx_less(sa, sb, dl))
+                ++ia;
+            else if (idx_less(sb, sa, dl))
+                ++ib;
+            else {
+                P.pair_a.push_back(t1.id[ia]);
+                P.pair_b.push_back(t2.id[ib]);
+                ++ia;
+                ++ib;
             }
-            if (P.pair_a.size() > first_pair) {
-                o.bidx.insert(o.bidx.end(), t1.k(ra.first), t1.k(ra.first) + nfa);
-                o.bidx.insert(o.bidx.end(), t2.k(rb.first), t2.k(rb.first) + nfb);
-                P.out_p0.push_back(int64_t(first_pair));
-                P.out_p1.push_back(int64_t(P.pair_a.size()));
+        }
+        if (P.pair_a.size() > first_pair) {
+            o.bidx.insert(o.bidx.end(), t1.k(ra.first), t1.k(ra.first) + nfa);
+            o.bidx.insert(o.bidx.end(), t2.k(rb.first), t2.k(rb.first) + nfb);
+            P.out_p0.push_back(int64_t(first_pair));
+            P.out_p1.push_back(int64_t(P.pair_a.size()));
+        }
+    };
+    if (dl == 0) {
+        for (auto &ra : r1)
+            for (auto &rb : r2) join(ra, rb);
+    } else {
+        // (suffix, run of B) for every block of B, sorted by suffix then run
+        std::vector<std::pair<size_t, int32_t>> sidx;  // (entry of t2, run)
+        sidx.reserve(t2.id.size());
+        for (size_t r = 0; r < r2.size(); ++r)
+            for (size_t i = r2[r].first; i < r2[r].second; ++i) sidx.push_back({i, int32_t(r)});
+        auto suf2 = [&](size_t i) { return t2.k(i) + nfb; };
+        std::sort(sidx.begin(), sidx.end(), [&](const auto &x, const auto &y) {
+            if (idx_less(suf2(x.first), suf2(y.first), dl)) return true;
+            if (idx_less(suf2(y.first), suf2(x.first), dl)) return false;
+            return x.second < y.second;
+        });
+        std::vector<int32_t> cand;
+        for (auto &ra : r1) {
+            cand.clear();
+            for (size_t ia = ra.first; ia < ra.second; ++ia) {
+                const int64_t *s = t1.k(ia) + nfa;
+                auto lo = std::lower_bound(sidx.begin(), sidx.end(), s,
+                                           [&](const auto &x, const int64_t *key) { return idx_less(suf2(x.first), key, dl); });
+                for (auto it = lo; it != sidx.end() && !idx_less(s, suf2(it->first), dl); ++it) cand.push_back(it->second);
             }
+            std::sort(cand.begin(), cand.end());
+            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+            for (int32_t rb : cand) join(ra, r2[rb]);
         }
     }
     o.boff.assign(P.out_p0.size(), 0);

@@ -162,3 +162,70 @@ def test_contraction_errors_map_to_reference_exceptions():
                     q.conserved.C5(0))
     with pytest.raises(ValueError, match="not allowed"):
         bad.set_block_structure([(1, 0)])
+
+
+def _legs_tensor(legs, mods, sel):
+    return o.fill(o.btensor(legs, sel, mods), np.zeros)
+
+
+@pytest.mark.parametrize("mods", [(0,), (0, 0), (3,)])
+def test_reshape_as_acceptance_matches_oracle(mods):
+    """reshape_as checks charge and size compatibility at every block position
+    (btensor.cpp:2876-2934); the library checks it group by group.  Both must accept
+    and reject the same layouts, including offsets that cancel across groups."""
+    rng = np.random.default_rng(31 + len(mods) + mods[0])
+    nc = len(mods)
+
+    def charge():
+        return tuple(int(rng.integers(0, m)) if m else int(rng.integers(-2, 3)) for m in mods)
+
+    def shift(c, s):
+        return tuple(((x + s) % m) if m else x + s for x, m in zip(c, mods))
+
+    zero = tuple(0 for _ in mods)
+    n = 0
+    for trial in range(60):
+        r = int(rng.integers(2, 5))
+        legs = [[(int(rng.integers(1, 4)), charge()) for _ in range(int(rng.integers(1, 4)))] for _ in range(r)]
+        T = _legs_tensor(legs, mods, zero)
+        if not T.blocks:
+            continue
+        split = int(rng.integers(1, r))
+        R = o.reshape(T, [split])
+        variants = []
+        # 1. the original layout (compatible)
+        variants.append(legs)
+        # 2. per-leg charge offsets that cancel across the split (compatible: every position's total is unchanged)
+        s = int(rng.integers(1, 3))
+        v = [[(sz, shift(c, s if d == 0 else 0)) for sz, c in leg] for d, leg in enumerate(legs)]
+        v[-1] = [(sz, shift(c, -s)) for sz, c in v[-1]]
+        variants.append(v)
+        # 3. one section's charge changed (incompatible unless the change is invisible)
+        v = [list(leg) for leg in legs]
+        d = int(rng.integers(0, r))
+        j = int(rng.integers(0, len(v[d])))
+        v[d][j] = (v[d][j][0], shift(v[d][j][1], 1))
+        variants.append(v)
+        # 4. two section sizes swapped between legs (sizes move between groups)
+        v = [list(leg) for leg in legs]
+        if len(v[0]) > 1:
+            v[0][0], v[0][1] = (v[0][1][0], v[0][0][1]), (v[0][0][0], v[0][1][1])
+        variants.append(v)
+        for lv in variants:
+            S = o.btensor(lv, zero, mods)
+            want = None
+            try:
+                o.reshape_as(R, S)
+            except ValueError as e:
+                want = str(e)
+            dR = to_device(R, True)
+            dS = q.btensor([[(sz, q.conserved.quantity(c, mods)) for sz, c in leg] for leg in lv],
+                           q.conserved.quantity(zero, mods))
+            got = None
+            try:
+                dR.reshape_as(dS)
+            except ValueError as e:
+                got = str(e)
+            assert (want is None) == (got is None), (legs, lv, want, got)
+            n += 1
+    assert n > 50
