@@ -51,9 +51,10 @@ def parse():
     p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving"],
+    p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving", "contraction"],
                    help="dmrg: the D=2048 sweep line (with a short serving section); serving: the full "
-                        "Poisson request stream of XXZ solves (L in 16..128, D in 32..512)")
+                        "Poisson request stream of XXZ solves (L in 16..128, D in 32..512); contraction: the "
+                        "synthetic theta-pair contraction + sector-SVD truncation microbench at D")
     p.add_argument("--serving-requests", type=int, default=16)
     p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate (requests/s)")
     p.add_argument("--serving-slots", type=int, default=8)
@@ -322,6 +323,76 @@ def serving_section(q, args, full):
     return out
 
 
+def contraction_workload(q, args):
+    """Synthetic block-sparse contraction + truncation: C[a,s,u,c] = A[a,s,t,b] B[b,t,u,c]
+    (bond legs of total D over U(1) charges -8..8, Gaussian section sizes, sigma 3),
+    reshaped to the charge-blocked (D*2) x (2*D) matrix and decomposed by sector SVD
+    truncated to D.  Each step runs both stages; L2 is flushed between steps."""
+    import torch
+    D = args.D
+    A, B = q.networks.theta_pair(D, seed=0)
+    stream = torch.cuda.ExternalStream(q.lib().qtt_get_stream())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    out = {}
+    for mode in ("f64", args.mode):
+        q.set_gemm_mode(mode)
+        try:
+            for _ in range(args.warmup):
+                C = A.tensordot(B, ([2, 3], [1, 0]))
+                q.linalg.svd(C, 2, 1e-10, min_size=1, max_size=D)
+            q.stats.reset()
+            q.stats.enable(True)
+            tc, ts = [], []
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                e0.record(stream)
+                C = A.tensordot(B, ([2, 3], [1, 0]))
+                e1.record(stream)
+                U, d, V = q.linalg.svd(C, 2, 1e-10, min_size=1, max_size=D)
+                e2.record(stream)
+                e2.synchronize()
+                tc.append(e0.elapsed_time(e1) / 1e3)
+                ts.append(e1.elapsed_time(e2) / 1e3)
+            kinds = {k: q.stats.get(k) for k in q.stats.KINDS}
+            q.stats.enable(False)
+            dv = np.sort(np.concatenate([v for _, v in d.blocks()]))[::-1]
+            out[mode] = {"contraction_s": float(np.mean(tc)), "truncation_s": float(np.mean(ts)),
+                         "total_s": float(np.mean(tc) + np.mean(ts)), "kinds": kinds, "C": C, "d": dv,
+                         "kept": int(len(dv))}
+        finally:
+            q.set_gemm_mode("f64")
+    m, f = out[args.mode], out["f64"]
+    # accuracy of the mixed path against the plain FP64 path on the same inputs
+    cm, cf = dict(m["C"].blocks()), dict(f["C"].blocks())
+    num = sum(float(np.sum((cm[k] - cf[k]) ** 2)) for k in cf)
+    den = sum(float(np.sum(cf[k] ** 2)) for k in cf)
+    nk = min(len(m["d"]), len(f["d"]))
+    P = peaks()
+    g = m["kinds"]["gemm"]
+    per_launch = g["ms"] / max(g["launches"], 1) / 1e3
+    achieved = g["work"] / max(g["launches"], 1) / per_launch / 1e12 if g["launches"] else 0.0
+    tf32_peak = P.get("bf16_tflops", 1939.7) / 2.0
+    return {"metric": "s per block-sparse contraction + sector-SVD truncation (theta pair at D)",
+            "value": m["total_s"], "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": m["total_s"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": f"{args.mode}+f32svd", "data": "synthetic",
+            "config": {"workload": f"theta-pair contraction C[a,s,u,c] = A[a,s,t,b] B[b,t,u,c] + svd(C, 2) "
+                                   f"truncated to {D}", "D": D, "charges": "U(1) -8..8, Gaussian sections sigma=3",
+                       "l2": "flushed between steps (256 MB write)", "seed": 0},
+            "contraction_s": m["contraction_s"], "truncation_s": m["truncation_s"],
+            "fp64": {"contraction_s": f["contraction_s"], "truncation_s": f["truncation_s"], "total_s": f["total_s"]},
+            "speedup_vs_fp64": f["total_s"] / m["total_s"],
+            "accuracy": {"C_rel_err": (num / den) ** 0.5, "d_max_rel_err": float(np.max(np.abs(m["d"][:nk] - f["d"][:nk])) / f["d"][0]),
+                         "kept_mixed": m["kept"], "kept_fp64": f["kept"]},
+            "roofline_gemm": {"kernel": "gemm", "bound": "tensor", "achieved": achieved, "peak": tf32_peak,
+                              "unit": "TFLOP/s", "frac": achieved / tf32_peak, "traffic": None,
+                              "per_launch_ms": per_launch * 1e3, "launches": g["launches"],
+                              "peak_source": "dense TF32 = 1/2 of MEASURED_PEAKS.json bf16_tflops (of measured)"},
+            "kernel_time_ms": {k: v["ms"] for k, v in m["kinds"].items()}}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -358,6 +429,13 @@ def main():
     import quantit_gb300 as q
     q.ensure_init(local)
     q.set_jacobi_kernel(args.jacobi)
+    if args.workload == "contraction":
+        line = contraction_workload(q, args)
+        if rank == 0:
+            print(json.dumps(line))
+        if world > 1:
+            dist.destroy_process_group()
+        return
     if args.workload == "serving":
         sv = serving_section(q, args, full=True)
         if rank == 0:

@@ -295,3 +295,41 @@ def random_bmps(L, D, phys_q=(1, -1), target=0, seed=0, mods=(0,)):
         blocks = [(k, v / nrm) for k, v in blocks]
         mps.append(from_blocks(legs, G.q(sel), blocks))
     return mps
+
+
+def gaussian_sections(D, qmax=8, sigma=3.0):
+    """Section sizes over charges -qmax..qmax from a Gaussian of width sigma,
+    rounded by largest remainders so that they sum to exactly D."""
+    qs = np.arange(-qmax, qmax + 1)
+    w = np.exp(-qs.astype(float) ** 2 / (2.0 * sigma * sigma))
+    raw = D * w / w.sum()
+    sizes = np.floor(raw).astype(int)
+    for i in np.argsort(-(raw - sizes), kind="stable")[:D - int(sizes.sum())]:
+        sizes[i] += 1
+    return [(int(n), int(q)) for n, q in zip(sizes, qs) if n > 0]
+
+
+def theta_pair(D, seed=0, qmax=8, sigma=3.0):
+    """The synthetic contraction operands: A[a, s, t, b] and B[b, t', u, c] with
+    bond legs of total D over U(1) charges -qmax..qmax (Gaussian section sizes),
+    spin-1/2 physical legs and N(0, 1) entries; A's legs (t, b) contract with B's
+    (t', b).  Returns (A, B)."""
+    rng = np.random.default_rng(seed)
+    bond = gaussian_sections(D, qmax, sigma)
+    phys = [(1, 1), (1, -1)]
+
+    def make(legs):
+        t = btensor([[(n, Z(q)) for n, q in leg] for leg in legs], Z(0))
+        charges = [[q for _, q in leg] for leg in legs]
+        sizes = [[n for n, _ in leg] for leg in legs]
+        blocks = []
+        for idx in itertools.product(*[range(len(c)) for c in charges]):
+            if sum(charges[d][j] for d, j in enumerate(idx)) == 0:
+                shp = tuple(sizes[d][j] for d, j in enumerate(idx))
+                blocks.append((idx, rng.standard_normal(shp)))
+        t.set_blocks(blocks)
+        return t
+
+    A = make([bond, phys, phys, [(n, -q) for n, q in bond]])
+    B = make([bond, [(n, -q) for n, q in phys], phys, [(n, -q) for n, q in bond]])
+    return A, B
