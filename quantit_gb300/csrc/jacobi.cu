@@ -350,6 +350,14 @@ struct BJacobiParams {
     int64_t max_steps;
     int *sweeps;   // per sector (written at the end)
     int *rotated;  // nsec * max_sweeps flags, zero on entry
+    // deferred V updates (null qbuf: each CTA updates V at the end of its block pair)
+    T *qbuf;       // 2 x max_jobs rotation matrices (NP x NP), by step parity
+    int *jobs;     // 2 x max_jobs x {sector, block a, block b, valid columns a | b << 16}
+    int *njobs;    // per step: jobs recorded (zero on entry)
+    int *vnext;    // per step: V work units claimed (zero on entry)
+    int max_jobs;  // >= block pairs per step
+    int upj;       // V work units (row chunks of one CTA width) per job
+    int max_q;     // widest sector (columns)
 };
 
 __device__ __forceinline__ int bj_items(int q, int B) {
@@ -471,6 +479,54 @@ __device__ __forceinline__ T bj_qdot(const T (&vr)[NP], const T *qcol) {
     return acc;
 }
 
+// V[r, cols] <- V[r, cols] Q for rows [r0, r1) of the 2B columns of blocks a and b
+// (na / nbc valid columns), Q = NP x NP column-major in shared memory.
+template <class T, int B>
+__device__ __forceinline__ void bj_apply_v(T *V, int q, int a, int b, int na, int nbc, const T *Qs, int r0, int r1,
+                                           int tid) {
+    constexpr int NP = 2 * B, NT = 32 * B;
+    auto valid = [&](int j) { return j < B ? j < na : (j - B) < nbc; };
+    auto column = [&](int j) { return j < B ? a * B + j : b * B + (j - B); };
+    for (int r = r0 + tid; r < r1; r += NT) {
+        T vr[NP];
+#pragma unroll
+        for (int j = 0; j < NP; ++j) vr[j] = valid(j) ? ldcg(V + int64_t(column(j)) * q + r) : T(0);
+#pragma unroll 2
+        for (int jp = 0; jp < NP; ++jp) {
+            if (!valid(jp)) continue;
+            V[int64_t(column(jp)) * q + r] = bj_qdot<T, NP>(vr, Qs + jp * NP);
+        }
+    }
+}
+
+// The deferred V updates of step `st`: CTAs claim (job, row chunk) units from a
+// counter until none are left, so CTAs without a block pair take most of them.
+template <class T, int B>
+__device__ void bj_vwork(const BJacobiParams<T> &P, int64_t st, T *Qs, int *s_unit, int tid) {
+    constexpr int NP = 2 * B, NT = 32 * B;
+    const int nj = __ldcg(P.njobs + st);
+    const int total = nj * P.upj;
+    const int par = int(st & 1);
+    for (;;) {
+        if (tid == 0) *s_unit = atomicAdd(P.vnext + st, 1);
+        __syncthreads();
+        const int u = *s_unit;
+        __syncthreads();
+        if (u >= total) break;
+        const int jb = u / P.upj, chunk = u - jb * P.upj;
+        const int *jr = P.jobs + (int64_t(par) * P.max_jobs + jb) * 4;
+        const int s = __ldcg(jr), a = __ldcg(jr + 1), b = __ldcg(jr + 2), nn = __ldcg(jr + 3);
+        const SectorDesc sd = P.secs[s];
+        const int r0 = chunk * NT;
+        if (r0 >= sd.q) continue;
+        const T *qsrc = P.qbuf + (int64_t(par) * P.max_jobs + jb) * NP * NP;
+        for (int e = tid; e < NP * NP; e += NT) Qs[e] = ldcg(qsrc + e);
+        __syncthreads();
+        bj_apply_v<T, B>(P.rot + sd.rot_off, sd.q, a, b, nn & 0xFFFF, nn >> 16, Qs, r0, min(sd.q, r0 + NT), tid);
+        __syncthreads();
+    }
+}
+
 template <class T, int B, int R>
 __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
     constexpr int NP = 2 * B;   // columns (players) of a block pair
@@ -485,8 +541,9 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
     int *done = reinterpret_cast<int *>(nrm + NP);
     int *sweep = done + nsec;
     int *istart = sweep + nsec;  // nsec + 1 prefix sums of block pairs per step
-    __shared__ int ndone, any_rot;
+    __shared__ int ndone, any_rot, s_unit;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool defer_v = P.qbuf != nullptr;
     const int64_t gt = int64_t(blockIdx.x) * NT + tid;
     const int64_t nt = int64_t(gridDim.x) * NT;
 
@@ -525,8 +582,10 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
     const int total = istart[nsec];
     grid.sync();
 
+    int64_t steps_run = 0;
     for (int64_t step = 0; step < P.max_steps; ++step) {
         if (ndone >= nsec) break;
+        steps_run = step + 1;
         for (int item = blockIdx.x; item < total; item += gridDim.x) {
             int lo = 0, hi = nsec - 1;
             while (lo < hi) {
@@ -561,11 +620,18 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             for (int j = warp; j < NP; j += B) {
                 if (!valid(j)) continue;
                 const T *src = W + int64_t(column(j)) * p;
+                // all R loads of a lane in flight at once (one L2 round trip per column)
+                T v[R];
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const int r = lane + 32 * i;
+                    v[i] = r < p ? ldcg(src + r) : T(0);
+                }
                 T acc = 0;
-                for (int r = lane; r < PP; r += 32) {
-                    const T v = r < p ? ldcg(src + r) : T(0);
-                    acc = fma(v, v, acc);
-                    cols[j * PP + r] = v;
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    acc = fma(v[i], v[i], acc);
+                    cols[j * PP + lane + 32 * i] = v[i];
                 }
                 acc = wsum(acc);
                 if (lane == 0) nrm[j] = acc;
@@ -646,22 +712,37 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                 for (int j = warp; j < NP; j += B) {
                     if (!valid(j)) continue;
                     T *dst = W + int64_t(column(j)) * p;
-                    for (int r = lane; r < p; r += 32) dst[r] = cols[j * PP + r];
-                }
-                for (int r = tid; r < q; r += NT) {
-                    T vr[NP];
 #pragma unroll
-                    for (int j = 0; j < NP; ++j) vr[j] = valid(j) ? ldcg(V + int64_t(column(j)) * q + r) : T(0);
-#pragma unroll 2
-                    for (int jp = 0; jp < NP; ++jp) {
-                        if (!valid(jp)) continue;
-                        V[int64_t(column(jp)) * q + r] = bj_qdot<T, NP>(vr, Qs + jp * NP);
+                    for (int i = 0; i < R; ++i) {
+                        const int r = lane + 32 * i;
+                        if (r < p) dst[r] = cols[j * PP + r];
                     }
+                }
+                if (defer_v) {
+                    // record Q and the job; the V update runs in the next step (bj_vwork)
+                    if (tid == 0) s_unit = atomicAdd(P.njobs + step, 1);
+                    __syncthreads();
+                    const int jb = s_unit;
+                    const int par = int(step & 1);
+                    T *qd = P.qbuf + (int64_t(par) * P.max_jobs + jb) * NP * NP;
+                    for (int e = tid; e < NP * NP; e += NT) qd[e] = Qs[e];
+                    if (tid == 0) {
+                        int *jr = P.jobs + (int64_t(par) * P.max_jobs + jb) * 4;
+                        jr[0] = s;
+                        jr[1] = a;
+                        jr[2] = b;
+                        jr[3] = na | (nbc << 16);
+                    }
+                } else {
+                    bj_apply_v<T, B>(V, q, a, b, na, nbc, Qs, 0, q, tid);
                 }
                 if (tid == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
             }
             __syncthreads();
         }
+        // the previous step's V updates: their columns are disjoint within that step,
+        // and the next step's updates of the same columns come after the next barrier
+        if (defer_v && step > 0) bj_vwork<T, B>(P, step - 1, Qs, &s_unit, tid);
         grid.sync();
         for (int s = tid; s < nsec; s += NT) {
             if (done[s]) continue;
@@ -679,6 +760,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
         }
         __syncthreads();
     }
+    if (defer_v && steps_run > 0) bj_vwork<T, B>(P, steps_run - 1, Qs, &s_unit, tid);
     if (blockIdx.x == 0)
         for (int s = tid; s < nsec; s += NT) P.sweeps[s] = sweep[s];
 }
@@ -832,8 +914,18 @@ constexpr size_t BJ_SMEM_MAX = 220 * 1024;  // dynamic shared memory of one bloc
 
 // false when the columns and the per-CTA sector tables (3 ints per sector) do not
 // fit one CTA's shared memory; the scalar kernel runs instead
+// Bytes of the deferred-V work area for block width B and element size es:
+// rotation matrices and job records for two steps, two counters per step.
+size_t bj_vwork_bytes(int B, size_t es, int nsec, int64_t sum_q, int64_t max_steps) {
+    const int64_t jobs = sum_q / (2 * B) + nsec;
+    const size_t np = size_t(2 * B);
+    return 2 * size_t(jobs) * np * np * es + 2 * size_t(jobs) * 4 * sizeof(int) + 2 * size_t(max_steps + 1) * sizeof(int) +
+           256;
+}
+
 template <class T, int B, int R>
-bool bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_q, cudaStream_t stream) {
+bool bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_q, void *vwork, size_t vwork_bytes,
+                    cudaStream_t stream) {
     const size_t smem = size_t(2 * B) * (32 * R + 2 * B + 1) * sizeof(T) + size_t(3 * P.nsec + 1) * sizeof(int);
     if (smem > BJ_SMEM_MAX) return false;
     static std::once_flag attr;
@@ -848,6 +940,25 @@ bool bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_
     if (occ < 1) fail(ERR_RUNTIME, "the block Jacobi kernel cannot be resident on an SM");
     BJacobiParams<T> Pc = P;
     Pc.max_steps = int64_t(P.max_sweeps) * std::max(1, max_block_steps) + 1;
+    Pc.qbuf = nullptr;
+    Pc.jobs = Pc.njobs = Pc.vnext = nullptr;
+    Pc.max_jobs = 0;
+    Pc.upj = 1;
+    const size_t need = bj_vwork_bytes(B, sizeof(T), P.nsec, sum_q, Pc.max_steps);
+    if (vwork && vwork_bytes >= need) {
+        // carve: counters first (zeroed here), then job records, then rotation matrices
+        const int64_t jobs = sum_q / (2 * B) + P.nsec;
+        char *w = static_cast<char *>(vwork);
+        const size_t cbytes = 2 * size_t(Pc.max_steps + 1) * sizeof(int);
+        Pc.njobs = reinterpret_cast<int *>(w);
+        Pc.vnext = Pc.njobs + (Pc.max_steps + 1);
+        Pc.jobs = reinterpret_cast<int *>(w + cbytes);
+        const size_t qoff = (cbytes + 2 * size_t(jobs) * 4 * sizeof(int) + 255) & ~size_t(255);
+        Pc.qbuf = reinterpret_cast<T *>(w + qoff);
+        Pc.max_jobs = int(jobs);
+        Pc.upj = std::max(1, int((P.max_q + 32 * B - 1) / (32 * B)));
+        cuda_check(cudaMemsetAsync(w, 0, cbytes, stream), "memset block-Jacobi counters");
+    }
     void *args[] = {&Pc};
     // block pairs per step: sum over sectors of ceil(ceil(q / B) / 2) <= sum_q / (2B) + nsec
     const int64_t items = sum_q / (2 * B) + P.nsec;
@@ -863,8 +974,8 @@ bool bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_
 // sectors as the shared-memory tables allow; returns false when the scalar kernel
 // has to run instead.
 template <class T>
-bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int max_p, int64_t sum_q,
-                      cudaStream_t stream) {
+bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int max_p, int64_t sum_q, void *vwork,
+                      size_t vwork_bytes, cudaStream_t stream) {
     const int max_qp = max_steps_per_sweep + 1;  // the widest sector's even column count
     auto steps = [&](int B) {
         const int nb = (max_qp + B - 1) / B;
@@ -872,40 +983,41 @@ bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int ma
     };
     if constexpr (sizeof(T) == 4) {
         if (max_p <= 4 * 32)
-            return bjacobi_launch<T, 16, 4>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 4>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 8 * 32)
-            return bjacobi_launch<T, 16, 8>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 8>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 16 * 32)
-            return bjacobi_launch<T, 16, 16>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 16>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 24 * 32)
-            return bjacobi_launch<T, 16, 24>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 24>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 32 * 32)
-            return bjacobi_launch<T, 16, 32>(P, steps(16), sum_q, stream);
+            return bjacobi_launch<T, 16, 32>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 48 * 32)
-            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 64 * 32)
-            return bjacobi_launch<T, 8, 64>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 64>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         return false;
     } else {
         if (max_p <= 4 * 32)
-            return bjacobi_launch<T, 8, 4>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 4>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 8 * 32)
-            return bjacobi_launch<T, 8, 8>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 8>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 16 * 32)
-            return bjacobi_launch<T, 8, 16>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 16>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 24 * 32)
-            return bjacobi_launch<T, 8, 24>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 24>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 32 * 32)
-            return bjacobi_launch<T, 8, 32>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 32>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         else if (max_p <= 48 * 32)
-            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, stream);
+            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
         return false;
     }
 }
 
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
-                 int max_sweeps, int *sweeps_out, int *flags, int max_p, int64_t sum_q, cudaStream_t stream) {
+                 int max_sweeps, int *sweeps_out, int *flags, int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes,
+                 cudaStream_t stream) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
@@ -919,7 +1031,8 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
         B.max_steps = 0;
         B.sweeps = sweeps_out;
         B.rotated = flags;
-        if (bjacobi_dispatch(B, max_steps_per_sweep, max_p, sum_q, stream)) return;
+        B.max_q = max_steps_per_sweep + 1;  // the widest sector's even column count bounds q
+        if (bjacobi_dispatch(B, max_steps_per_sweep, max_p, sum_q, vwork, vwork_bytes, stream)) return;
     }
     JacobiParams<T> P;
     P.work = work;
@@ -984,21 +1097,32 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p, int64_t sum_q) {
+                      int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes) {
     if (nsec <= 0) return;
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
-                    max_sweeps, sweeps_out, flags, max_p, sum_q, stream);
+                    max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes, stream);
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
-                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, stream);
+                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes, stream);
 }
 
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
-                   int64_t sum_q) {
+                   int64_t sum_q, void *vwork, size_t vwork_bytes) {
     launch_jacobi_on(ctx().stream, work, rot, sec, slot_start, nsec, max_steps_per_sweep, max_sweeps, sweeps_out, flags,
-                     f32, max_p, sum_q);
+                     f32, max_p, sum_q, vwork, vwork_bytes);
+}
+
+size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int max_sweeps, int f32) {
+    const size_t es = f32 ? 4 : 8;
+    size_t best = 0;
+    for (int B : {8, 16}) {
+        const int nb = (max_steps_per_sweep + 1 + B - 1) / B;
+        const int64_t steps = int64_t(max_sweeps) * std::max(1, nb + (nb & 1) - 1) + 1;
+        best = std::max(best, bj_vwork_bytes(B, es, nsec, sum_q, steps));
+    }
+    return best;
 }
 
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,

@@ -162,9 +162,13 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 // sweeps_out[s] receives the number of sweeps sector s used; flags holds
 // nsec*max_sweeps ints of scratch.
 // sum_q: the sectors' total column count (sizes the cooperative grid to the work).
+// vwork (optional, jacobi_vwork_bytes): lets the block kernel defer each step's V
+// updates to the next step, where CTAs without a block pair run them; without it
+// every CTA updates V right after its block pair.
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
-                   int64_t sum_q);
+                   int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0);
+size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int max_sweeps, int f32);
 // Column norms, sort (descending for svd, ascending eigenvalues for eigh),
 // normalisation and completion of null columns; writes U (m x k), V (n x k)
 // column-major and s (k) per sector in FP64, k = min(m, n).  max_q: largest q;
@@ -174,7 +178,7 @@ void launch_finish(const void *work, const void *rot, double *U, double *V, doub
 // The same two launches on an explicit stream (no library context involved).
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p, int64_t sum_q);
+                      int max_p, int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0);
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
                       const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32);
 // Segment = one output block (rows x k row-major at dst_off) from a column-major

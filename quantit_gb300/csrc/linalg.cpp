@@ -262,7 +262,10 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     }
     {
         StatScope sc(ST_SVD, 0.0);
-        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot);
+        const size_t vb = jacobi_vwork_bytes(nsec, stot, max_steps, max_sweeps, f32);
+        BufPtr vwork = dev_alloc(vb);
+        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
+                      vwork->p, vb);
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
                       static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32);
     }
