@@ -43,9 +43,11 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--model", default="heisenberg", choices=["heisenberg", "hubbard"],
+    p.add_argument("--model", default="heisenberg", choices=["heisenberg", "hubbard", "cylinder"],
                    help="heisenberg: spin-1/2 chain, U(1) (defaults L=32, D=2048); hubbard: Fermi-Hubbard "
-                        "U=8 at half filling, U(1)xU(1) (defaults L=64, D=1024)")
+                        "U=8 at half filling, U(1)xU(1) (defaults L=64, D=1024); cylinder: spin-1/2 Heisenberg "
+                        "on a 12 x 6 open cylinder, snake order (72 sites, long-range MPO; default D=512, "
+                        "reached by a bond-dimension ramp)")
     p.add_argument("--L", type=int, default=None)
     p.add_argument("--D", type=int, default=None)
     p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3"])
@@ -122,7 +124,10 @@ def peaks():
 
 
 def build_state(q, L, D, seed=0, model="heisenberg"):
-    if model == "hubbard":
+    if model == "cylinder":
+        mpo = q.networks.cylinder_heisenberg(12, 6, 1.0, "snake")
+        mps = q.networks.random_bmps(len(mpo), D, seed=seed)
+    elif model == "hubbard":
         mpo = q.networks.hubbard(L, 8.0)
         mps = q.networks.random_bmps(L, D, q.networks.HUBBARD_PHYS, (L, 0), seed=seed, mods=(0, 0))
     else:
@@ -397,11 +402,17 @@ def main():
     args = parse()
     rank, world, local = dist_env()
     hub = args.model == "hubbard"
+    cyl = args.model == "cylinder"
     if args.L is None:
-        args.L = 64 if hub else 32
+        args.L = 72 if cyl else (64 if hub else 32)
     if args.D is None:
-        args.D = 1024 if hub else 2048
-    if hub:
+        args.D = 512 if cyl else (1024 if hub else 2048)
+    if cyl:
+        cfg = {"workload": f"Heisenberg 12x6 open cylinder (snake order, 72 sites), two-site DMRG sweep at "
+                           f"D={args.D} after a ramp from D={max(64, args.D // 4)}, U(1) Sz=0",
+               "L": 72, "D": args.D, "model": "spin-1/2 Heisenberg J=1 on an open cylinder Lx=12 x Ly=6 "
+                                               "(periodic around Ly), long-range MPO w=35"}
+    elif hub:
         cfg = {"workload": f"Fermi-Hubbard chain L={args.L}, U=8, half filling, two-site DMRG sweep at D={args.D}, "
                            "U(1)xU(1) (N, 2Sz)", "L": args.L, "D": args.D,
                "model": "Fermi-Hubbard open chain t=1 U=8 mu=0, N=L, Sz=0"}
@@ -414,9 +425,9 @@ def main():
            "parallelism": "replicas only" if world > 1 else "single GPU"})
     if args.impl == "reference":
         if rank == 0:
-            if hub:
+            if hub or cyl:
                 print(json.dumps({"impl": "reference", "unavailable": "the CPU sampler restates the Heisenberg "
-                                  "bond update only; the Hubbard model runs on the GPU paths"}))
+                                  "chain's bond update only; this model runs on the GPU paths"}))
             else:
                 print(json.dumps(reference_arm(args, cfg)))
         return
@@ -450,6 +461,10 @@ def main():
             dist.destroy_process_group()
         return
     mpo, mps0 = build_state(q, args.L, args.D, seed=rank, model=args.model)
+    if cyl:  # bond-dimension ramp (one sweep per stage) before the sweeps at D
+        for Dr in (max(64, args.D // 4), max(64, args.D // 2)):
+            if Dr < args.D:
+                _, _, mps0 = run_sweeps(q, mpo, mps0, 1, args.mode, Dr)
     _, _, mps1 = run_sweeps(q, mpo, mps0, args.warmup, args.mode, args.D)
     q.stats.reset()
     q.stats.enable(True)
@@ -495,7 +510,7 @@ def main():
             "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e}
     if cmp:
         line["vs_fp64"] = cmp
-    if rank == 0 and not args.no_cpu_baseline and hub:
+    if rank == 0 and not args.no_cpu_baseline and (hub or cyl):
         line["cpu_baseline"] = None  # the oracle sampler restates the Heisenberg bond update only
     elif rank == 0 and not args.no_cpu_baseline:
         try:
@@ -507,7 +522,7 @@ def main():
                                               f"x {s.factor:.1f} size-weighted bonds per sweep"}
         except Exception as e:  # reported, never hidden
             line["cpu_baseline"] = {"error": repr(e)}
-    if rank == 0 and args.serving_requests > 0 and not hub:
+    if rank == 0 and args.serving_requests > 0 and not (hub or cyl):
         try:
             line["serving"] = serving_section(q, args, full=False)
         except Exception as e:  # reported, never hidden

@@ -333,3 +333,86 @@ def theta_pair(D, seed=0, qmax=8, sigma=3.0):
     A = make([bond, phys, phys, [(n, -q) for n, q in bond]])
     B = make([bond, [(n, -q) for n, q in phys], phys, [(n, -q) for n, q in bond]])
     return A, B
+
+
+def heisenberg_couplings_dense(L, couplings):
+    """Dense site tensors W_i[a, s, b, s'] of H = sum_(i<j) J_ij S_i.S_j for arbitrary
+    pair couplings, as a finite-state automaton on the spin-1/2 basis {up, down}
+    (the local layout of Heisenberg_impl, sources/models.cpp:38-68: the left edge
+    takes the last row, the right edge the first column).  States: 0 = every term
+    finished; 1 + 3 (d - 1) + o = operator o in (S+, S-, Sz) placed d sites to the
+    left (d = 1 .. the longest coupling); last = nothing placed yet.  A coupling
+    J_ij is placed as S_i^o at site i and closed with its partner at site j."""
+    pairs = {}
+    dmax = 0
+    for i, j, J in couplings:
+        i, j = int(min(i, j)), int(max(i, j))
+        if i == j or not (0 <= i < L and 0 <= j < L):
+            raise ValueError("couplings need two different sites of the chain")
+        pairs[(i, j)] = pairs.get((i, j), 0.0) + float(J)
+        dmax = max(dmax, j - i)
+    sp = np.array([[0.0, 1.0], [0.0, 0.0]])   # S+ on (up, down)
+    sm = sp.T
+    sz = np.diag([0.5, -0.5])
+    idm = np.eye(2)
+    ops = (sp, sm, sz)
+    partner = (0.5 * sm, 0.5 * sp, sz)        # S.S = (S+S- + S-S+)/2 + SzSz
+    n = 2 + 3 * dmax
+    start = n - 1
+    ws = []
+    for k in range(L):
+        w = np.zeros((n, 2, n, 2))
+        w[0, :, 0, :] = idm
+        w[start, :, start, :] = idm
+        if any(i == k for (i, j) in pairs):
+            for o in range(3):
+                w[start, :, 1 + o, :] = ops[o]
+        for d in range(1, dmax + 1):
+            for o in range(3):
+                a = 1 + 3 * (d - 1) + o
+                if d < dmax:
+                    w[a, :, a + 3, :] = idm
+                J = pairs.get((k - d, k))
+                if J:
+                    w[a, :, 0, :] = J * partner[o]
+        ws.append(w)
+    ws[0] = ws[0][start:start + 1]
+    ws[-1] = ws[-1][:, :, 0:1]
+    return ws
+
+
+def heisenberg_couplings(L, couplings):
+    """Block MPO (U(1) 2Sz charges) of heisenberg_couplings_dense."""
+    return dense_mpo_to_bmpo(heisenberg_couplings_dense(L, couplings), [1, -1])
+
+
+def cylinder_sites(Lx, Ly, order="snake"):
+    """Chain position of lattice site (x, y) of an Lx (open) x Ly (periodic) cylinder:
+    column by column, every other column reversed for ``snake``."""
+    pos = {}
+    for x in range(Lx):
+        for y in range(Ly):
+            yy = (Ly - 1 - y) if (order == "snake" and x % 2) else y
+            pos[(x, y)] = x * Ly + yy
+    return pos
+
+
+def cylinder_couplings(Lx, Ly, J=1.0, order="snake"):
+    """Nearest-neighbour pairs of the Lx x Ly cylinder (periodic around Ly) as chain
+    couplings (i, j, J)."""
+    pos = cylinder_sites(Lx, Ly, order)
+    out = set()
+    for x in range(Lx):
+        for y in range(Ly):
+            a = pos[(x, y)]
+            nbrs = [(x, (y + 1) % Ly)] + ([(x + 1, y)] if x + 1 < Lx else [])
+            for nb in nbrs:
+                b = pos[nb]
+                if a != b:
+                    out.add((min(a, b), max(a, b)))
+    return [(i, j, J) for i, j in sorted(out)]
+
+
+def cylinder_heisenberg(Lx, Ly, J=1.0, order="snake"):
+    """Spin-1/2 Heisenberg model on an Lx x Ly open cylinder, H = J sum_<ij> S_i.S_j."""
+    return heisenberg_couplings(Lx * Ly, cylinder_couplings(Lx, Ly, J, order))

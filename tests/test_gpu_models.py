@@ -73,3 +73,41 @@ def test_hubbard_mixed_matches_fp64():
         e, n2 = q.algorithms.mps_energy(mpo, cur)
         out[gemm] = e / n2
     assert abs(out["tf32x3"] - out["f64"]) / L < 1e-8, out
+
+
+def test_cylinder_dmrg_matches_oracle():
+    """Long-range MPO (4x3 snake cylinder, couplings up to distance 5): the GPU DMRG
+    follows the oracle sweep for sweep."""
+    mpo = NET.cylinder_heisenberg(4, 3, 1.0, "snake")
+    L, D = len(mpo), 16
+    mps = NET.random_bmps(L, D, seed=6)
+    mpo_o = [to_oracle(t) for t in mpo]
+    mps_o = [to_oracle(t) for t in mps]
+    log = q.algorithms.dmrg_log_sweeptime()
+    dmps = NET.bMPS([to_device(t) for t in mps_o], mps.orthogonality_center)
+    q.algorithms.dmrg(mpo, dmps, q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=D,
+                                                           min_bond=2, maximum_iterations=3), log)
+    E2, oc2, Es2 = o.dmrg(mpo_o, mps_o, mps.orthogonality_center,
+                          o.DmrgOptions(cutoff=1e-10, convergence_criterion=0.0, maximum_bond=D, minimum_bond=2,
+                                        maximum_iterations=3))
+    np.testing.assert_allclose(log.energies, Es2, rtol=1e-10)
+    for a, b in zip(dmps, mps_o):
+        assert same_structure(a, b)
+        assert a.block_indices() == [k for k, _ in b.blocks]
+
+
+def test_cylinder_mixed_matches_fp64():
+    mpo = NET.cylinder_heisenberg(4, 4, 1.0, "snake")
+    L, D = len(mpo), 64
+    mps = NET.random_bmps(L, D, seed=7)
+    mps.move_oc(0)
+    mps.normalize_center()
+    base = dict(cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=1)
+    q.algorithms.dmrg(mpo, mps, q.algorithms.dmrg_options(maximum_iterations=8, gemm="f64", **base))
+    out = {}
+    for gemm in ("f64", "tf32x3"):
+        cur = NET.bMPS(list(mps), mps.orthogonality_center)
+        q.algorithms.dmrg(mpo, cur, q.algorithms.dmrg_options(maximum_iterations=2, gemm=gemm, **base))
+        e, n2 = q.algorithms.mps_energy(mpo, cur)
+        out[gemm] = e / n2
+    assert abs(out["tf32x3"] - out["f64"]) / L < 1e-8, out

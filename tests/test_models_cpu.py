@@ -109,3 +109,54 @@ def test_product_charge_bond_sectors():
             assert 0 <= nr <= 2 * (L - b - 1) and abs(sz) <= nr
     # the U(1) interface is unchanged: integer keys
     assert all(isinstance(k, int) for k in networks.bond_sectors(8, 16, [1, -1], 0)[3])
+
+
+def _energy_dense(ws, mps):
+    env = np.ones((1, 1, 1))
+    for W, A in zip(ws, mps):
+        env = np.einsum("abc,bsBt,asx,ctz->xBz", env, W, A, A, optimize=True)
+    nrm = np.ones((1, 1))
+    for A in mps:
+        nrm = np.einsum("ac,asx,csz->xz", nrm, A, A)
+    return env.reshape(-1)[0] / nrm.reshape(-1)[0]
+
+
+def test_coupling_mpo_matches_reference_cylinder_fixture():
+    """The reference's 4x8 Heisenberg cylinder MPO (tests/2dHeisenberg of the reference,
+    converted by tests/golden/make_cylinder_fixture.py) is column-major with columns of
+    8 periodic sites and J = 1 on 55 bonds (the last column's wrap bond 24-31 is absent
+    from the fixture).  The automaton builder given that coupling list is the same
+    operator: equal <psi|H|psi> on random MPS, same bond dimension."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "heisenberg_cylinder_4x8_mpo.npz"))
+    fix = [z[f"w{i}"][:, ::-1, :, ::-1] for i in range(32)]  # fixture basis {down, up} -> {up, down}
+    cp = [c for c in networks.cylinder_couplings(4, 8, 1.0, "column") if (c[0], c[1]) != (24, 31)]
+    assert len(cp) == 55
+    ws = networks.heisenberg_couplings_dense(32, cp)
+    assert max(w.shape[0] for w in ws) == max(w.shape[0] for w in fix) == 26
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        dims = [1] + [4] * 31 + [1]
+        mps = [rng.standard_normal((dims[i], 2, dims[i + 1])) for i in range(32)]
+        assert _energy_dense(ws, mps) == pytest.approx(_energy_dense(fix, mps), rel=1e-12, abs=1e-12)
+
+
+@pytest.mark.parametrize("Lx, Ly, order", [(2, 3, "snake"), (3, 2, "column"), (2, 4, "snake")])
+def test_cylinder_mpo_matches_direct_hamiltonian(Lx, Ly, order):
+    L = Lx * Ly
+    cp = networks.cylinder_couplings(Lx, Ly, 1.0, order)
+    Hm = _mpo_matrix(networks.heisenberg_couplings_dense(L, cp))
+    sx = np.array([[0, .5], [.5, 0]])
+    sy = np.array([[0, -.5j], [.5j, 0]])
+    sz = np.diag([.5, -.5])
+
+    def op(a, i):
+        m = np.eye(1)
+        for j in range(L):
+            m = np.kron(m, a if j == i else np.eye(2))
+        return m
+    H = sum(J * (op(sx, i) @ op(sx, j) + op(sy, i) @ op(sy, j) + op(sz, i) @ op(sz, j)).real for i, j, J in cp)
+    np.testing.assert_allclose(Hm, H, atol=1e-12)
+    # geometry: every site has its 3 (or 4) neighbours, the snake keeps columns contiguous
+    pos = networks.cylinder_sites(Lx, Ly, order)
+    assert sorted(pos.values()) == list(range(L))
