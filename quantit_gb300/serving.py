@@ -25,12 +25,15 @@ from . import _lib, algorithms, networks
 
 
 class SolveRequest:
-    """One ground-state request: XXZ chain of length L, anisotropy delta, bond dimension D."""
+    """One ground-state request: XXZ chain of length L, anisotropy delta, bond dimension
+    D; ``resume`` names a block-list file (serialize.save) holding the MPS to start from
+    instead of the seeded random one."""
 
-    __slots__ = ("rid", "L", "delta", "D", "seed", "arrival")
+    __slots__ = ("rid", "L", "delta", "D", "seed", "arrival", "resume")
 
-    def __init__(self, rid, L, delta, D, seed, arrival=0.0):
+    def __init__(self, rid, L, delta, D, seed, arrival=0.0, resume=None):
         self.rid, self.L, self.delta, self.D, self.seed, self.arrival = rid, int(L), float(delta), int(D), int(seed), float(arrival)
+        self.resume = resume
 
 
 class SolveResult:
@@ -103,19 +106,30 @@ def device_memory():
     return f.value, t.value
 
 
-def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10):
-    """One request on the calling thread: build the MPO and the seeded random MPS,
-    bring the MPS to canonical form (move_oc(0) and normalisation, in FP64: a raw
-    random MPS's environments shrink like D^-i and leave the FP64 range on long
-    chains), run two-site DMRG to the relative energy convergence, return (E, sweeps)."""
+def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, checkpoint_dir=None):
+    """One request on the calling thread: build the MPO and the seeded random MPS (or
+    read the request's checkpoint), bring the MPS to canonical form (move_oc(0) and
+    normalisation, in FP64: a raw random MPS's environments shrink like D^-i and
+    leave the FP64 range on long chains), run two-site DMRG to the relative energy
+    convergence, write the optimised MPS to ``checkpoint_dir`` when given, return
+    (E, sweeps)."""
+    from . import serialize
     mpo = networks.xxz(req.L, req.delta)
-    mps = networks.random_bmps(req.L, req.D, seed=req.seed)
+    if getattr(req, "resume", None):
+        mps = serialize.load(req.resume)
+        if len(mps) != req.L:
+            raise ValueError("the checkpoint's length differs from the request's")
+    else:
+        mps = networks.random_bmps(req.L, req.D, seed=req.seed)
     mps.move_oc(0)
     mps.normalize_center()
     opts = algorithms.dmrg_options(cutoff=cutoff, convergence_criterion=convergence, max_bond=req.D, min_bond=1,
                                    maximum_iterations=max_sweeps, gemm=gemm, final_energy_fp64=True)
     log = algorithms.dmrg_log_sweeptime()
     E = algorithms.dmrg(mpo, mps, opts, log)
+    if checkpoint_dir:
+        import os
+        serialize.save(os.path.join(checkpoint_dir, f"request_{req.rid}.npz"), mps)
     return E, len(log.energies)
 
 
@@ -123,12 +137,14 @@ class ServingEngine:
     """Admission by slots and memory footprint, worker threads with one stream each."""
 
     def __init__(self, slots=8, memory_budget=None, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10,
-                 device=0, solver=None, footprint=None):
+                 device=0, solver=None, footprint=None, checkpoint_dir=None):
         if slots < 1:
             raise ValueError("a serving engine needs at least one slot")
         self.slots = int(slots)
         self.device = int(device)
         self.solve_args = dict(gemm=gemm, convergence=convergence, max_sweeps=max_sweeps, cutoff=cutoff)
+        if checkpoint_dir:
+            self.solve_args["checkpoint_dir"] = checkpoint_dir
         # solver(req, **solve_args) -> (E, sweeps); the default is the GPU solve
         self.solver = solver or solve
         self.footprint = footprint or (lambda r: footprint_bytes(r.L, r.D))
