@@ -204,7 +204,9 @@ __device__ __forceinline__ void load_tile(const float *__restrict__ hi, const fl
 #pragma unroll
     for (int i = 0; i < (ROWS * (TBK / 4)) / TTHREADS; ++i) {
         const int e = tid + i * TTHREADS;
-        const int row = e >> 3, kc = e & 7;
+        // eight consecutive threads take eight consecutive rows of one core matrix
+        // (one contiguous 128-byte store per quarter warp, no bank conflicts)
+        const int row = ((e >> 6) << 3) | (e & 7), kc = (e >> 3) & 7;
         const int gr = row0 + row, gk = k0 + kc * 4;
         uint4 vh = make_uint4(0, 0, 0, 0), vl = make_uint4(0, 0, 0, 0);
         if (gr < rows_valid && gk < K4) {
