@@ -167,6 +167,10 @@ typedef struct {
                                       instead of the last Ritz value -- after every sweep for the
                                       convergence test and the log when convergence_criterion > 0,
                                       and for the returned energy (default 1) */
+    int32_t lanczos_steps;         /* 1: QuantiT's one-step update (two_sites_update, dmrg.cpp:624-638);
+                                      k > 1: k-step Lanczos with full reorthogonalisation (no
+                                      reference counterpart; default 1) */
+    int32_t reserved;              /* zero */
 } qtt_dmrg_options;
 /* dmrg_options defaults (include/dmrg_options.h:15-58) */
 void qtt_dmrg_options_default(qtt_dmrg_options *opt);

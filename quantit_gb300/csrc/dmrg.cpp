@@ -53,6 +53,116 @@ void eig2x2(double a0, double a1, double b, double &E, double &o, double &n) {
     if (std::isnan(o) || std::isnan(n)) fail(ERR_LOGIC, "nan found in output tensor");
 }
 
+namespace {
+// Lowest eigenpair of a small dense symmetric matrix (row-major n x n) by cyclic
+// Jacobi rotations in FP64 (n is the Krylov dimension, at most a few dozen).
+void small_sym_lowest(std::vector<double> A, int n, double &lam, std::vector<double> &vec) {
+    std::vector<double> V(size_t(n) * n, 0.0);
+    for (int i = 0; i < n; ++i) V[size_t(i) * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                const double x = A[size_t(i) * n + j] * A[size_t(i) * n + j];
+                tot += x;
+                if (i != j) off += x;
+            }
+        if (off <= 1e-30 * tot || off == 0.0) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[size_t(p) * n + q];
+                if (apq == 0.0) continue;
+                const double app = A[size_t(p) * n + p], aqq = A[size_t(q) * n + q];
+                const double th = (aqq - app) / (2.0 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int r = 0; r < n; ++r) {  // A <- A J (columns p, q)
+                    const double x = A[size_t(r) * n + p], y = A[size_t(r) * n + q];
+                    A[size_t(r) * n + p] = c * x - s * y;
+                    A[size_t(r) * n + q] = s * x + c * y;
+                }
+                for (int r = 0; r < n; ++r) {  // A <- J^T A (rows p, q)
+                    const double x = A[size_t(p) * n + r], y = A[size_t(q) * n + r];
+                    A[size_t(p) * n + r] = c * x - s * y;
+                    A[size_t(q) * n + r] = s * x + c * y;
+                }
+                for (int r = 0; r < n; ++r) {
+                    const double x = V[size_t(r) * n + p], y = V[size_t(r) * n + q];
+                    V[size_t(r) * n + p] = c * x - s * y;
+                    V[size_t(r) * n + q] = s * x + c * y;
+                }
+            }
+    }
+    int best = 0;
+    for (int i = 1; i < n; ++i)
+        if (A[size_t(i) * n + i] < A[size_t(best) * n + best]) best = i;
+    lam = A[size_t(best) * n + best];
+    vec.assign(n, 0.0);
+    for (int r = 0; r < n; ++r) vec[r] = V[size_t(r) * n + best];
+}
+}  // namespace
+
+// k-step Lanczos on the two-site effective Hamiltonian.  Not a QuantiT function:
+// an optional replacement of its one-step update (dmrg_options lanczos_steps > 1)
+// that converges a bond in one visit instead of many sweeps.  Every coefficient
+// (alpha, beta, the two-pass Gram-Schmidt projections) stays a device scalar, so
+// the k matvecs run without a host synchronisation; one download then feeds the
+// k x k tridiagonal Ritz problem, solved on the host in FP64.  A Krylov breakdown
+// (beta below 1e-13 of the largest |alpha|) truncates the Ritz problem there.
+LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R, int k) {
+    if (k < 1) fail(ERR_INVALID_ARGUMENT, "lanczos_steps must be at least 1");
+    DevScratch scr;
+    double *a = scr.get(size_t(k)), *b = scr.get(size_t(k)), *c = scr.get(1), *n0 = scr.get(1);
+    std::vector<BT> V;
+    dot_all_dev(state, state, n0, scr);
+    launch_sqrt(n0);
+    V.push_back(scale_dev(state, Coef{1.0, n0, 1, 0, 1e-300}));
+    for (int j = 0; j < k; ++j) {
+        BT w = hamil2site_times_state(V[j], hamil, L, R);
+        dot_all_dev(V[j], w, a + j, scr);
+        w = add_scaled_dev(w, V[j], coef_host(1.0), Coef{-1.0, a + j, 0, 0, 0.0});
+        if (j > 0) w = add_scaled_dev(w, V[j - 1], coef_host(1.0), Coef{-1.0, b + j - 1, 0, 0, 0.0});
+        for (int pass = 0; pass < 2; ++pass)
+            for (int i = 0; i <= j; ++i) {
+                dot_all_dev(V[i], w, c, scr);
+                w = add_scaled_dev(w, V[i], coef_host(1.0), Coef{-1.0, c, 0, 0, 0.0});
+            }
+        if (j + 1 == k) break;
+        dot_all_dev(w, w, b + j, scr);
+        launch_sqrt(b + j);
+        V.push_back(scale_dev(w, Coef{1.0, b + j, 1, 0, 1e-300}));
+    }
+    std::vector<double> ha(k), hb(k);
+    cuda_check(cudaMemcpyAsync(ha.data(), a, size_t(k) * 8, cudaMemcpyDeviceToHost, ctx().stream), "Lanczos alpha");
+    if (k > 1)
+        cuda_check(cudaMemcpyAsync(hb.data(), b, size_t(k - 1) * 8, cudaMemcpyDeviceToHost, ctx().stream),
+                   "Lanczos beta");
+    cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+    double scale = 0.0;
+    for (int j = 0; j < k; ++j) {
+        if (std::isnan(ha[j]) || (j + 1 < k && std::isnan(hb[j]))) fail(ERR_LOGIC, "nan found in output tensor");
+        scale = std::max(scale, std::fabs(ha[j]));
+    }
+    int m = k;
+    for (int j = 0; j + 1 < k; ++j)
+        if (!(hb[j] > 1e-13 * std::max(scale, 1e-300))) {
+            m = j + 1;
+            break;
+        }
+    std::vector<double> T(size_t(m) * m, 0.0);
+    for (int j = 0; j < m; ++j) {
+        T[size_t(j) * m + j] = ha[j];
+        if (j + 1 < m) T[size_t(j) * m + j + 1] = T[size_t(j + 1) * m + j] = hb[j];
+    }
+    LanczosKOut o;
+    std::vector<double> y;
+    small_sym_lowest(T, m, o.E, y);
+    o.psi = scale_dev(V[0], coef_host(y[0]));
+    for (int j = 1; j < m; ++j) o.psi = add_scaled_dev(o.psi, V[j], coef_host(1.0), coef_host(y[j]));
+    o.dim = m;
+    return o;
+}
+
 // scal layout: [0] a0, [1] b, [2] a1, [3] E, [4] o, [5] n, [6] nan flag
 LanczosOut one_step_lanczos_dev(const BT &state, const BT &hamil, const BT &L, const BT &R, double *scal,
                                 DevScratch &scr) {
@@ -201,11 +311,19 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
             DevScratch scr;
             double *scal = scr.get(8);
             BT theta = tensordot(mps[oc], mps[oc + 1], {2}, {0});
-            LanczosOut lz = one_step_lanczos_dev(theta, h2[oc], env[oc], env[oc + 3], scal, scr);
-            launch_eig2x2(scal);
-            BT upd = add_scaled_dev(theta, lz.psi, Coef{1.0, scal + 4, 0, 0, 0.0}, Coef{1.0, scal + 5, 0, 0, 0.0});
-            cuda_check(cudaMemcpyAsync(hscal, scal, 7 * sizeof(double), cudaMemcpyDeviceToHost, ctx().stream),
-                       "cudaMemcpyAsync(scalars)");
+            BT upd;
+            if (opt.lanczos_steps > 1) {
+                LanczosKOut lk = lanczos_k(theta, h2[oc], env[oc], env[oc + 3], opt.lanczos_steps);
+                upd = lk.psi;
+                hscal[3] = lk.E;
+                hscal[6] = 0.0;
+            } else {
+                LanczosOut lz = one_step_lanczos_dev(theta, h2[oc], env[oc], env[oc + 3], scal, scr);
+                launch_eig2x2(scal);
+                upd = add_scaled_dev(theta, lz.psi, Coef{1.0, scal + 4, 0, 0, 0.0}, Coef{1.0, scal + 5, 0, 0, 0.0});
+                cuda_check(cudaMemcpyAsync(hscal, scal, 7 * sizeof(double), cudaMemcpyDeviceToHost, ctx().stream),
+                           "cudaMemcpyAsync(scalars)");
+            }
             SVDOut f = svd_truncated(upd, 2, opt.cutoff, opt.minimum_bond, opt.maximum_bond, 2.0);  // syncs
             if (hscal[6] != 0.0) fail(ERR_LOGIC, "nan found in output tensor");
             E = hscal[3];

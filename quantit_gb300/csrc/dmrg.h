@@ -15,7 +15,16 @@ struct DmrgOpts {
     int64_t maximum_iterations = 1000;
     int gemm_mode = GEMM_F64;
     int final_energy_fp64 = 1;  // mixed modes: return the FP64 <psi|H|psi>/<psi|psi> of the final state
+    int lanczos_steps = 1;      // 1: QuantiT's one-step update; k > 1: k-step Lanczos (lanczos_k)
 };
+// k-step Lanczos with full reorthogonalisation: the lowest Ritz value and its
+// (normalised) Ritz vector of the two-site effective Hamiltonian.
+struct LanczosKOut {
+    BT psi;
+    double E = 0.0;
+    int dim = 0;  // Krylov dimension used (smaller than k after a breakdown)
+};
+LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R, int k);
 typedef void (*DmrgLog)(void *user, int64_t sweep, double energy, double seconds);
 
 struct LanczosOut {
