@@ -170,7 +170,8 @@ typedef struct {
     int32_t lanczos_steps;         /* 1: QuantiT's one-step update (two_sites_update, dmrg.cpp:624-638);
                                       k > 1: k-step Lanczos with full reorthogonalisation (no
                                       reference counterpart; default 1) */
-    int32_t reserved;              /* zero */
+    int32_t cuda_graphs;           /* k-step Lanczos: capture the two-site matvec once per bond as a CUDA
+                                      graph and replay it for the remaining iterations (default 1) */
 } qtt_dmrg_options;
 /* dmrg_options defaults (include/dmrg_options.h:15-58) */
 void qtt_dmrg_options_default(qtt_dmrg_options *opt);

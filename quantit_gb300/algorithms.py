@@ -12,7 +12,8 @@ class dmrg_options:
     """dmrg_options (include/dmrg_options.h:15-58) plus the block-GEMM precision."""
 
     def __init__(self, *, cutoff=1e-6, convergence_criterion=1e-5, max_bond=SIZE_MAX, min_bond=4,
-                 maximum_iterations=1000, gemm="f64", final_energy_fp64=True, lanczos_steps=1):
+                 maximum_iterations=1000, gemm="f64", final_energy_fp64=True, lanczos_steps=1,
+                 cuda_graphs=True):
         self.cutoff = cutoff
         self.convergence_criterion = convergence_criterion
         self.maximum_bond = max_bond
@@ -24,6 +25,8 @@ class dmrg_options:
         self.final_energy_fp64 = final_energy_fp64
         # 1: QuantiT's one-step update; k > 1: k-step Lanczos per bond
         self.lanczos_steps = lanczos_steps
+        # k-step Lanczos: replay each bond's matvec from a captured CUDA graph
+        self.cuda_graphs = cuda_graphs
 
     def _c(self):
         o = _lib.DmrgOptionsC()
@@ -35,6 +38,7 @@ class dmrg_options:
         o.gemm_mode = GEMM_MODES[self.gemm] if isinstance(self.gemm, str) else int(self.gemm)
         o.final_energy_fp64 = int(bool(self.final_energy_fp64))
         o.lanczos_steps = int(self.lanczos_steps)
+        o.cuda_graphs = int(bool(self.cuda_graphs))
         return o
 
 

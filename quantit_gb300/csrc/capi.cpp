@@ -364,7 +364,7 @@ void qtt_dmrg_options_default(qtt_dmrg_options *o) {
     o->gemm_mode = QTT_GEMM_F64;
     o->final_energy_fp64 = 1;
     o->lanczos_steps = 1;
-    o->reserved = 0;
+    o->cuda_graphs = 1;
 }
 int qtt_compute_2sites_hamil(qtt_bt wl, qtt_bt wr, qtt_bt *out) {
     return guarded([&] {
@@ -431,6 +431,7 @@ int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_d
             o.gemm_mode = opt->gemm_mode;
             o.final_energy_fp64 = opt->final_energy_fp64;
             o.lanczos_steps = opt->lanczos_steps > 0 ? opt->lanczos_steps : 1;
+            o.cuda_graphs = opt->cuda_graphs;
         }
         *E0 = qtt::dmrg(W, S, *oc, o, log_fn, log_user);
         for (int i = 0; i < L; ++i) mps[i] = wrap(std::move(S[i]));

@@ -100,6 +100,93 @@ void small_sym_lowest(std::vector<double> A, int n, double &lam, std::vector<dou
     vec.assign(n, 0.0);
     for (int r = 0; r < n; ++r) vec[r] = V[size_t(r) * n + best];
 }
+bool same_layout(const BT &a, const BT &b) {
+    return a.rank == b.rank && a.dt == b.dt && a.nnz == b.nnz && a.sbd == b.sbd && a.ssz == b.ssz &&
+           a.bidx == b.bidx && a.boff == b.boff;
+}
+
+// t's structure in a buffer of its own, filled by a device copy of `src` (same layout)
+BT copy_layout(const BT &t, const void *src) {
+    BT o = t.shape_only();
+    o.sel = t.sel;
+    o.bidx = t.bidx;
+    o.boff = t.boff;
+    o.nnz = t.nnz;
+    o.alloc_data();
+    if (t.nnz)
+        cuda_check(cudaMemcpyAsync(o.data(), src, size_t(t.nnz) * dsize(t.dt), cudaMemcpyDeviceToDevice,
+                                   ctx().stream),
+                   "cudaMemcpyAsync(copy)");
+    return o;
+}
+
+// The two-site matvec captured once as a CUDA graph and replayed for every Krylov
+// vector of the same block layout: the host planning of its three contractions
+// (merge-joins, tile and split tables) and their launches are paid once per bond
+// instead of once per Lanczos iteration.  The graph reads its input from X and
+// writes its output into graph-owned memory (instantiated with auto-free on launch,
+// so every launch reuses the same address); run() copies it out.
+struct GraphedMatvec {
+    cudaGraphExec_t exec = nullptr;
+    BT X, Y;
+    void *yptr = nullptr;
+    bool launched = false;
+    int64_t launches = 0;
+    std::vector<void *> tables;
+
+    bool capture(const BT &v, const BT &hamil, const BT &L, const BT &R) {
+        Ctx &c = ctx();
+        X = copy_layout(v, v.data());
+        const int64_t l0 = launch_count();
+        c.capturing = true;
+        c.capture_tables = &tables;
+        cudaGraph_t g = nullptr;
+        bool ok = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+        if (ok) {
+            try {
+                Y = hamil2site_times_state(X, hamil, L, R);
+            } catch (...) {
+                ok = false;
+            }
+            ok = (cudaStreamEndCapture(c.stream, &g) == cudaSuccess) && ok;
+        }
+        c.capturing = false;
+        c.capture_tables = nullptr;
+        if (ok) ok = cudaGraphInstantiateWithFlags(&exec, g, cudaGraphInstantiateFlagAutoFreeOnLaunch) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        if (!ok || !Y.has_data) {
+            exec = nullptr;
+            Y = BT();
+            return false;
+        }
+        launches = launch_count() - l0;
+        // Y's memory belongs to the graph: detach it from the tensor's owner
+        yptr = Y.buf->p;
+        Y.buf->p = nullptr;
+        return true;
+    }
+    BT run(const BT &v) {
+        Ctx &c = ctx();
+        if (v.nnz)
+            cuda_check(cudaMemcpyAsync(X.data(), v.data(), size_t(v.nnz) * dsize(v.dt), cudaMemcpyDeviceToDevice,
+                                       c.stream),
+                       "cudaMemcpyAsync(graph input)");
+        cuda_check(cudaGraphLaunch(exec, c.stream), "cudaGraphLaunch");
+        launched = true;
+        count_launch(int(launches));
+        return copy_layout(Y, yptr);
+    }
+    ~GraphedMatvec() {
+        Ctx &c = ctx();
+        if (launched && yptr) cudaFreeAsync(yptr, c.stream);
+        if (exec) {
+            cudaStreamSynchronize(c.stream);
+            cudaGraphExecDestroy(exec);
+        }
+        for (void *p : tables) cudaFree(p);
+    }
+};
 }  // namespace
 
 // k-step Lanczos on the two-site effective Hamiltonian.  Not a QuantiT function:
@@ -109,8 +196,10 @@ void small_sym_lowest(std::vector<double> A, int n, double &lam, std::vector<dou
 // the k matvecs run without a host synchronisation; one download then feeds the
 // k x k tridiagonal Ritz problem, solved on the host in FP64.  A Krylov breakdown
 // (beta below 1e-13 of the largest |alpha|) truncates the Ritz problem there.
-LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R, int k) {
+LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R, int k, bool graphs) {
     if (k < 1) fail(ERR_INVALID_ARGUMENT, "lanczos_steps must be at least 1");
+    GraphedMatvec gm;
+    bool graph_ok = graphs;
     DevScratch scr;
     double *a = scr.get(size_t(k)), *b = scr.get(size_t(k)), *c = scr.get(1), *n0 = scr.get(1);
     std::vector<BT> V;
@@ -118,7 +207,20 @@ LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R
     launch_sqrt(n0);
     V.push_back(scale_dev(state, Coef{1.0, n0, 1, 0, 1e-300}));
     for (int j = 0; j < k; ++j) {
-        BT w = hamil2site_times_state(V[j], hamil, L, R);
+        BT w;
+        if (graph_ok && gm.exec && same_layout(V[j], gm.X)) {
+            w = gm.run(V[j]);
+        } else if (graph_ok && !gm.exec && j >= 1 && j + 1 < k && same_layout(V[j], V[j - 1])) {
+            // the Krylov vectors' layout has settled: capture once, replay from here on
+            if (gm.capture(V[j], hamil, L, R))
+                w = gm.run(V[j]);
+            else {
+                graph_ok = false;
+                w = hamil2site_times_state(V[j], hamil, L, R);
+            }
+        } else {
+            w = hamil2site_times_state(V[j], hamil, L, R);
+        }
         dot_all_dev(V[j], w, a + j, scr);
         w = add_scaled_dev(w, V[j], coef_host(1.0), Coef{-1.0, a + j, 0, 0, 0.0});
         if (j > 0) w = add_scaled_dev(w, V[j - 1], coef_host(1.0), Coef{-1.0, b + j - 1, 0, 0, 0.0});
@@ -313,7 +415,7 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
             BT theta = tensordot(mps[oc], mps[oc + 1], {2}, {0});
             BT upd;
             if (opt.lanczos_steps > 1) {
-                LanczosKOut lk = lanczos_k(theta, h2[oc], env[oc], env[oc + 3], opt.lanczos_steps);
+                LanczosKOut lk = lanczos_k(theta, h2[oc], env[oc], env[oc + 3], opt.lanczos_steps, opt.cuda_graphs != 0);
                 upd = lk.psi;
                 hscal[3] = lk.E;
                 hscal[6] = 0.0;

@@ -16,6 +16,7 @@ struct DmrgOpts {
     int gemm_mode = GEMM_F64;
     int final_energy_fp64 = 1;  // mixed modes: return the FP64 <psi|H|psi>/<psi|psi> of the final state
     int lanczos_steps = 1;      // 1: QuantiT's one-step update; k > 1: k-step Lanczos (lanczos_k)
+    int cuda_graphs = 1;        // k-step Lanczos: replay the matvec from a captured CUDA graph
 };
 // k-step Lanczos with full reorthogonalisation: the lowest Ritz value and its
 // (normalised) Ritz vector of the two-site effective Hamiltonian.
@@ -24,7 +25,7 @@ struct LanczosKOut {
     double E = 0.0;
     int dim = 0;  // Krylov dimension used (smaller than k after a breakdown)
 };
-LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R, int k);
+LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R, int k, bool graphs = true);
 typedef void (*DmrgLog)(void *user, int64_t sweep, double energy, double seconds);
 
 struct LanczosOut {

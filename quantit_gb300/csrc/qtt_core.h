@@ -144,6 +144,10 @@ struct Ctx {
     // error word of this thread's tensor-core launches (bounded waits that expired)
     int *tc_err = nullptr;
     bool tc_used = false;
+    // set while a CUDA graph is being captured on this stream: uploads go to
+    // dedicated device buffers (constants of the graph) and statistics are off
+    bool capturing = false;
+    std::vector<void *> *capture_tables = nullptr;
 };
 Ctx &ctx();
 void set_stream(cudaStream_t s);

@@ -80,6 +80,15 @@ BufPtr dev_alloc(size_t bytes) {
 void *upload(const void *host, size_t bytes) {
     Ctx &c = ctx();
     size_t need = (bytes + 255) & ~size_t(255);
+    if (c.capturing) {
+        // a captured graph replays its kernels long after this call: its tables live in
+        // their own buffers, filled now (relaxed capture mode allows the synchronous copy)
+        void *d = nullptr;
+        cuda_check(cudaMalloc(&d, std::max<size_t>(need, 256)), "cudaMalloc(graph table)");
+        c.capture_tables->push_back(d);
+        cuda_check(cudaMemcpy(d, host, bytes, cudaMemcpyHostToDevice), "cudaMemcpy(graph table)");
+        return d;
+    }
     if (need > c.ring_bytes / 2) fail(ERR_RUNTIME, "planning table larger than the staging ring");
     size_t half = c.ring_bytes / 2;
     size_t half_end = (c.cur_half + 1) * half;
@@ -142,7 +151,7 @@ void stats_defer_work(int kind, std::function<double()> f) {
 }
 bool stats_enabled() { return g_stats_on; }
 StatScope::StatScope(int k, double w) : kind(k), work(w) {
-    if (!g_stats_on) return;
+    if (!g_stats_on || ctx().capturing) return;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx().stream);
