@@ -58,8 +58,12 @@ def parse():
                         "Poisson request stream of XXZ solves (L in 16..128, D in 32..512); contraction: the "
                         "synthetic theta-pair contraction + sector-SVD truncation microbench at D")
     p.add_argument("--serving-requests", type=int, default=16)
-    p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate (requests/s)")
+    p.add_argument("--serving-rate", type=float, default=4.0,
+                   help="Poisson arrival rate (requests/s); above the service capacity the stream measures the "
+                        "saturated throughput and its queueing latency")
     p.add_argument("--serving-slots", type=int, default=8)
+    p.add_argument("--serving-lanczos", type=int, default=4,
+                   help="Lanczos steps per bond in the serving solves (1: QuantiT's one-step update)")
     p.add_argument("--serving-fp64-every", type=int, default=4,
                    help="serial FP64 baseline on every k-th request of the stream")
     p.add_argument("--serving-fp64-budget", type=float, default=300.0,
@@ -298,13 +302,14 @@ def serving_section(q, args, full):
     dist = SERVING_FULL if full else SERVING_REDUCED
     reqs = serving.poisson_requests(args.serving_requests, rate=args.serving_rate, seed=0, **dist)
     eng = serving.ServingEngine(slots=args.serving_slots, gemm=args.mode if args.mode != "f64" else "tf32x3",
-                                convergence=1e-8, max_sweeps=40)
+                                convergence=1e-8, max_sweeps=40, lanczos_steps=args.serving_lanczos)
     res = eng.run(reqs, realtime=True)
     mk = max(r.done for r in res) - min(r.arrival for r in res)
     out = serving.summarize([r.latency for r in res], mk, len(res))
     out.update({"requests": len(reqs), "rate_per_s": args.serving_rate, "slots": args.serving_slots,
                 "distribution": {"L": list(dist["lengths"]), "D": list(dist["bonds"]), "delta": [0.0, 2.0]},
-                "convergence": 1e-8, "gemm": "tf32x3", "peak_concurrency": eng.peak_concurrency,
+                "convergence": 1e-8, "gemm": "tf32x3", "lanczos_steps": args.serving_lanczos,
+                "peak_concurrency": eng.peak_concurrency,
                 "memory_budget_bytes": eng.memory_budget, "peak_admitted_bytes": eng.peak_memory,
                 "errors": sum(1 for r in res if r.error),
                 "mean_service_s": float(np.mean([r.service for r in res])),
@@ -314,7 +319,8 @@ def serving_section(q, args, full):
     for r in reqs[::max(1, args.serving_fp64_every)]:
         if sample and time.perf_counter() - t0 > args.serving_fp64_budget:
             break
-        st += serving.serial_solve_times([r], gemm="f64", convergence=1e-8, max_sweeps=40)
+        st += serving.serial_solve_times([r], gemm="f64", convergence=1e-8, max_sweeps=40,
+                                         lanczos_steps=args.serving_lanczos)
         sample.append(r)
     svc = [x[0] for x in st]
     mixed = {r.rid: r for r in res}

@@ -106,12 +106,13 @@ def device_memory():
     return f.value, t.value
 
 
-def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, checkpoint_dir=None):
+def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, checkpoint_dir=None, lanczos_steps=4):
     """One request on the calling thread: build the MPO and the seeded random MPS (or
     read the request's checkpoint), bring the MPS to canonical form (move_oc(0) and
     normalisation, in FP64: a raw random MPS's environments shrink like D^-i and
     leave the FP64 range on long chains), run two-site DMRG to the relative energy
-    convergence, write the optimised MPS to ``checkpoint_dir`` when given, return
+    convergence (``lanczos_steps``-step Lanczos per bond, matvecs replayed from CUDA
+    graphs), write the optimised MPS to ``checkpoint_dir`` when given, return
     (E, sweeps)."""
     from . import serialize
     mpo = networks.xxz(req.L, req.delta)
@@ -124,7 +125,8 @@ def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, che
     mps.move_oc(0)
     mps.normalize_center()
     opts = algorithms.dmrg_options(cutoff=cutoff, convergence_criterion=convergence, max_bond=req.D, min_bond=1,
-                                   maximum_iterations=max_sweeps, gemm=gemm, final_energy_fp64=True)
+                                   maximum_iterations=max_sweeps, gemm=gemm, final_energy_fp64=True,
+                                   lanczos_steps=lanczos_steps)
     log = algorithms.dmrg_log_sweeptime()
     E = algorithms.dmrg(mpo, mps, opts, log)
     if checkpoint_dir:
@@ -137,12 +139,13 @@ class ServingEngine:
     """Admission by slots and memory footprint, worker threads with one stream each."""
 
     def __init__(self, slots=8, memory_budget=None, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10,
-                 device=0, solver=None, footprint=None, checkpoint_dir=None):
+                 device=0, solver=None, footprint=None, checkpoint_dir=None, lanczos_steps=4):
         if slots < 1:
             raise ValueError("a serving engine needs at least one slot")
         self.slots = int(slots)
         self.device = int(device)
-        self.solve_args = dict(gemm=gemm, convergence=convergence, max_sweeps=max_sweeps, cutoff=cutoff)
+        self.solve_args = dict(gemm=gemm, convergence=convergence, max_sweeps=max_sweeps, cutoff=cutoff,
+                               lanczos_steps=lanczos_steps)
         if checkpoint_dir:
             self.solve_args["checkpoint_dir"] = checkpoint_dir
         # solver(req, **solve_args) -> (E, sweeps); the default is the GPU solve
