@@ -466,7 +466,8 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return
-    mpo, mps0 = build_state(q, args.L, args.D, seed=rank, model=args.model)
+    from quantit_gb300 import replicas
+    mpo, mps0 = build_state(q, args.L, args.D, seed=replicas.replica_seed(0, rank), model=args.model)
     if cyl:  # bond-dimension ramp (one sweep per stage) before the sweeps at D
         for Dr in (max(64, args.D // 4), max(64, args.D // 2)):
             if Dr < args.D:
@@ -489,10 +490,11 @@ def main():
     kinds = {k: q.stats.get(k) for k in q.stats.KINDS}
     q.stats.enable(False)
     t_step = float(np.mean(ts))
-    if world > 1:
-        t = torch.tensor([wall, t_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall, t_step = float(t[0].item()), float(t[1].item())
+    # replicas: the slowest rank's times; the whole job's seconds per sweep divide the
+    # slowest rank's sweep time by the sweeps all ranks ran in it
+    from quantit_gb300 import replicas
+    wall, t_step = replicas.max_over_ranks([wall, t_step])
+    job_per_sweep = t_step / world
     E_mixed, t_eval = fp64_energy(q, mpo, mps2)
     cmp = None
     if args.mode != "f64" and args.compare_f64:
@@ -505,7 +507,7 @@ def main():
     P = peaks()
     pc = {}
     dom = max(kinds, key=lambda k: kinds[k]["ms"])
-    line = {"metric": METRIC, "value": t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    line = {"metric": METRIC, "value": job_per_sweep, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f32svd+f64",
             "data": "synthetic", "config": dict(cfg, mode=args.mode, jacobi=args.jacobi), "ritz_energies": Es,
