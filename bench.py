@@ -518,6 +518,7 @@ def main():
             "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e}
     if cmp:
         line["vs_fp64"] = cmp
+    line["autotune"] = q.autotune_report().splitlines()
     if rank == 0 and not args.no_cpu_baseline and (hub or cyl):
         line["cpu_baseline"] = None  # the oracle sampler restates the Heisenberg bond update only
     elif rank == 0 and not args.no_cpu_baseline:

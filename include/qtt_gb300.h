@@ -66,6 +66,13 @@ int qtt_synchronize(void);
 /* Block-GEMM precision for the calling process (QTT_GEMM_*). */
 int qtt_set_gemm_mode(int mode);
 int qtt_get_gemm_mode(void);
+/* Block-width autotuner of the sector-SVD kernel (no reference counterpart): on by
+ * default; the first decompositions of each class (precision, column length, widest
+ * sector, sector count) time the candidate widths and keep the faster.
+ * QTT_AUTOTUNE_FILE persists the decisions.  The report lists them, one per line;
+ * *len receives its length. */
+int qtt_set_autotune(int on);
+int qtt_autotune_report(char *buf, int64_t cap, int64_t *len);
 /* Free and total bytes of the calling thread's device (no reference counterpart;
  * the serving loop admits solves against it). */
 int qtt_device_memory(int64_t *free_bytes, int64_t *total_bytes);

@@ -19,6 +19,23 @@ def set_gemm_mode(mode):
     call("qtt_set_gemm_mode", algorithms.GEMM_MODES[mode] if isinstance(mode, str) else int(mode))
 
 
+def set_autotune(on):
+    """Turn the sector-SVD block-width autotuner on (default) or off."""
+    from ._lib import call
+    call("qtt_set_autotune", 1 if on else 0)
+
+
+def autotune_report():
+    """The autotuner's decisions, one line per class of decomposition."""
+    import ctypes as C
+    from ._lib import call
+    n = C.c_int64()
+    call("qtt_autotune_report", None, 0, C.byref(n))
+    buf = C.create_string_buffer(n.value + 1)
+    call("qtt_autotune_report", buf, n.value + 1, C.byref(n))
+    return buf.value.decode()
+
+
 def set_jacobi_kernel(which):
     """Sector-SVD Jacobi kernel: 'block' (block-cyclic wherever it fits, the
     default) or 'scalar' (one column pair per warp and grid step)."""

@@ -36,6 +36,8 @@ SIGNATURES = {
     "qtt_synchronize": (C.c_int, []),
     "qtt_set_gemm_mode": (C.c_int, [C.c_int]),
     "qtt_set_jacobi_kernel": (C.c_int, [C.c_int]),
+    "qtt_set_autotune": (C.c_int, [C.c_int]),
+    "qtt_autotune_report": (C.c_int, [C.c_char_p, i64, P(i64)]),
     "qtt_device_memory": (C.c_int, [P(i64), P(i64)]),
     "qtt_get_gemm_mode": (C.c_int, []),
     "qtt_bt_create": (C.c_int, [i32, P(i64), P(i64), i32, P(C.c_uint16), P(C.c_int16), P(C.c_int16), i32, P(bt)]),

@@ -93,6 +93,20 @@ int qtt_device_memory(int64_t *free_bytes, int64_t *total_bytes) {
         *total_bytes = int64_t(t);
     });
 }
+int qtt_set_autotune(int on) {
+    return guarded([&] { qtt::set_autotune(on); });
+}
+int qtt_autotune_report(char *buf, int64_t cap, int64_t *len) {
+    return guarded([&] {
+        const std::string r = qtt::autotune_report();
+        if (len) *len = int64_t(r.size());
+        if (buf && cap > 0) {
+            const size_t n = std::min<size_t>(r.size(), size_t(cap - 1));
+            std::memcpy(buf, r.data(), n);
+            buf[n] = 0;
+        }
+    });
+}
 int qtt_set_jacobi_kernel(int which) {
     return guarded([&] { qtt::set_jacobi_variant(which); });
 }

@@ -13,7 +13,14 @@
 // Every loop is bounded: at most max_sweeps sweeps per sector.
 #include <cooperative_groups.h>
 
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
 #include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
 
 #include "kernels.h"
 #include "qtt_core.h"
@@ -970,47 +977,99 @@ bool bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_
     return true;
 }
 
+// Register slice (elements per lane and column) for columns of at most max_p.
+int r_class(int max_p) {
+    for (int R : {4, 8, 16, 24, 32, 48, 64})
+        if (max_p <= 32 * R) return R;
+    return 0;
+}
+
+// Block widths the block kernel is built with for (element type, R): FP32 16 (R <= 32)
+// and 8 (R <= 64); FP64 8 (R <= 48) and 16 (R <= 8, beyond that 16 warps run out of
+// registers).  The first entry is the default.
+std::vector<int> block_widths(bool f32, int R) {
+    if (R == 0) return {};
+    if (f32) return R <= 32 ? std::vector<int>{16, 8} : std::vector<int>{8};
+    if (R > 48) return {};
+    return R <= 8 ? std::vector<int>{8, 16} : std::vector<int>{8};
+}
+
 // Block kernel for columns up to 2048 (FP32) / 1536 (FP64) elements, as many
-// sectors as the shared-memory tables allow; returns false when the scalar kernel
-// has to run instead.
+// sectors as the shared-memory tables allow, block width B (one of block_widths);
+// returns false when the scalar kernel has to run instead.
 template <class T>
 bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int max_p, int64_t sum_q, void *vwork,
-                      size_t vwork_bytes, cudaStream_t stream) {
+                      size_t vwork_bytes, int B, cudaStream_t stream) {
     const int max_qp = max_steps_per_sweep + 1;  // the widest sector's even column count
-    auto steps = [&](int B) {
-        const int nb = (max_qp + B - 1) / B;
+    auto steps = [&](int b) {
+        const int nb = (max_qp + b - 1) / b;
         return nb + (nb & 1) - 1;
     };
+    const int R = r_class(max_p);
+#define QTT_BJ(BB, RR)                                                                                            \
+    if (B == BB && R == RR) return bjacobi_launch<T, BB, RR>(P, steps(BB), sum_q, vwork, vwork_bytes, stream);
     if constexpr (sizeof(T) == 4) {
-        if (max_p <= 4 * 32)
-            return bjacobi_launch<T, 16, 4>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 8 * 32)
-            return bjacobi_launch<T, 16, 8>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 16 * 32)
-            return bjacobi_launch<T, 16, 16>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 24 * 32)
-            return bjacobi_launch<T, 16, 24>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 32 * 32)
-            return bjacobi_launch<T, 16, 32>(P, steps(16), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 48 * 32)
-            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 64 * 32)
-            return bjacobi_launch<T, 8, 64>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        return false;
+        QTT_BJ(16, 4) QTT_BJ(16, 8) QTT_BJ(16, 16) QTT_BJ(16, 24) QTT_BJ(16, 32)
+        QTT_BJ(8, 4) QTT_BJ(8, 8) QTT_BJ(8, 16) QTT_BJ(8, 24) QTT_BJ(8, 32) QTT_BJ(8, 48) QTT_BJ(8, 64)
     } else {
-        if (max_p <= 4 * 32)
-            return bjacobi_launch<T, 8, 4>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 8 * 32)
-            return bjacobi_launch<T, 8, 8>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 16 * 32)
-            return bjacobi_launch<T, 8, 16>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 24 * 32)
-            return bjacobi_launch<T, 8, 24>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 32 * 32)
-            return bjacobi_launch<T, 8, 32>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        else if (max_p <= 48 * 32)
-            return bjacobi_launch<T, 8, 48>(P, steps(8), sum_q, vwork, vwork_bytes, stream);
-        return false;
+        QTT_BJ(8, 4) QTT_BJ(8, 8) QTT_BJ(8, 16) QTT_BJ(8, 24) QTT_BJ(8, 32) QTT_BJ(8, 48)
+        QTT_BJ(16, 4) QTT_BJ(16, 8)
+    }
+#undef QTT_BJ
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner of the block width.  Decompositions are classed by element type, R,
+// the widest sector (power-of-two bucket) and the sector count (power-of-two
+// bucket) -- the shape of the skewed sector-size distribution that decides whether
+// wide blocks (fewer grid steps) or narrow ones (more block pairs in flight, fewer
+// rounds per step) win.  The first calls of a class run every candidate width
+// twice, timed with CUDA events on the launching stream; the faster width is used
+// for the class from then on.  QTT_AUTOTUNE_FILE names a file the decisions are
+// read from at first use and appended to.
+struct TuneKey {
+    int f32, R, qcls, ncls;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(f32, R, qcls, ncls) < std::tie(o.f32, o.R, o.qcls, o.ncls);
+    }
+};
+struct TuneState {
+    int tried[2] = {0, 0};
+    float best_ms[2] = {1e30f, 1e30f};
+    int winner = -1;  // index into block_widths()
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneState> g_tune;
+std::atomic<int> g_autotune{1};
+bool g_tune_loaded = false;
+constexpr int TUNE_TRIALS = 2;
+
+int ceil_log2(int64_t x) {
+    int b = 0;
+    while ((int64_t(1) << b) < x) ++b;
+    return b;
+}
+
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = std::getenv("QTT_AUTOTUNE_FILE");
+    if (!path) return;
+    if (FILE *f = std::fopen(path, "r")) {
+        TuneKey k;
+        int w;
+        while (std::fscanf(f, "%d %d %d %d %d", &k.f32, &k.R, &k.qcls, &k.ncls, &w) == 5) g_tune[k].winner = w;
+        std::fclose(f);
+    }
+}
+
+void tune_save(const TuneKey &k, int w) {
+    const char *path = std::getenv("QTT_AUTOTUNE_FILE");
+    if (!path) return;
+    if (FILE *f = std::fopen(path, "a")) {
+        std::fprintf(f, "%d %d %d %d %d\n", k.f32, k.R, k.qcls, k.ncls, w);
+        std::fclose(f);
     }
 }
 
@@ -1032,7 +1091,50 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
         B.sweeps = sweeps_out;
         B.rotated = flags;
         B.max_q = max_steps_per_sweep + 1;  // the widest sector's even column count bounds q
-        if (bjacobi_dispatch(B, max_steps_per_sweep, max_p, sum_q, vwork, vwork_bytes, stream)) return;
+        const bool f32 = sizeof(T) == 4;
+        const std::vector<int> cands = block_widths(f32, r_class(max_p));
+        if (!cands.empty()) {
+            int ci = 0;
+            bool timing = false;
+            const TuneKey key{f32 ? 1 : 0, r_class(max_p), ceil_log2(max_steps_per_sweep + 1), ceil_log2(nsec)};
+            if (g_autotune.load() && cands.size() > 1) {
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                tune_load_locked();
+                TuneState &st = g_tune[key];
+                if (st.winner >= 0 && st.winner < int(cands.size())) {
+                    ci = st.winner;
+                } else {
+                    ci = st.tried[1] < st.tried[0] ? 1 : 0;
+                    timing = true;
+                }
+            }
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (timing) {
+                cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+                cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+                cuda_check(cudaEventRecord(e0, stream), "cudaEventRecord");
+            }
+            const bool ok = bjacobi_dispatch(B, max_steps_per_sweep, max_p, sum_q, vwork, vwork_bytes, cands[ci], stream);
+            if (timing) {
+                float ms = 0.f;
+                cuda_check(cudaEventRecord(e1, stream), "cudaEventRecord");
+                cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+                cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                if (ok) {
+                    std::lock_guard<std::mutex> lk(g_tune_mu);
+                    TuneState &st = g_tune[key];
+                    st.tried[ci] += 1;
+                    st.best_ms[ci] = std::min(st.best_ms[ci], ms);
+                    if (st.winner < 0 && st.tried[0] >= TUNE_TRIALS && st.tried[1] >= TUNE_TRIALS) {
+                        st.winner = st.best_ms[1] < st.best_ms[0] ? 1 : 0;
+                        tune_save(key, st.winner);
+                    }
+                }
+            }
+            if (ok) return;
+        }
     }
     JacobiParams<T> P;
     P.work = work;
@@ -1141,4 +1243,27 @@ void launch_finish(const void *work, const void *rot, double *U, double *V, doub
     launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32);
 }
 
+}  // namespace qtt
+
+namespace qtt {
+void set_autotune(int on) { g_autotune = on ? 1 : 0; }
+std::string autotune_report() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    std::string out;
+    char line[160];
+    for (auto &kv : g_tune) {
+        const TuneKey &k = kv.first;
+        const TuneState &st = kv.second;
+        const std::vector<int> c = block_widths(k.f32 != 0, k.R);
+        char t0[32] = "-", t1[32] = "-";
+        if (st.tried[0]) std::snprintf(t0, sizeof(t0), "%.3f", st.best_ms[0]);
+        if (st.tried[1]) std::snprintf(t1, sizeof(t1), "%.3f", st.best_ms[1]);
+        std::snprintf(line, sizeof(line), "%s R=%d max_q<=2^%d nsec<=2^%d: B=%d (%s; B=%d %s ms, B=%d %s ms)\n",
+                      k.f32 ? "fp32" : "fp64", k.R, k.qcls, k.ncls,
+                      st.winner >= 0 && st.winner < int(c.size()) ? c[st.winner] : (c.empty() ? 0 : c[0]),
+                      st.winner >= 0 ? "tuned" : "tuning", c.size() > 0 ? c[0] : 0, t0, c.size() > 1 ? c[1] : 0, t1);
+        out += line;
+    }
+    return out;
+}
 }  // namespace qtt

@@ -311,6 +311,9 @@ struct ScopedGemmMode {
 // (one column pair per warp and grid step).
 void set_jacobi_variant(int v);
 int jacobi_variant();
+// Block-width autotuner of the block-Jacobi kernel (on by default) and its decisions.
+void set_autotune(int on);
+std::string autotune_report();
 // Non-zero when a tensor-core kernel gave up on a bounded wait since the last
 // check (synchronises the device; read and cleared).
 int tc_error_check();

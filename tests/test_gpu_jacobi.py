@@ -97,3 +97,16 @@ def test_block_and_scalar_kernels_agree():
     b = _svd_with(t, "scalar", "f64")
     for x, y in zip(a[1].blocks(), b[1].blocks()):
         np.testing.assert_allclose(x[1], y[1], rtol=0, atol=1e-13 * max(float(np.max(y[1])), 1e-300))
+
+
+def test_autotuner_times_both_widths_and_results_stay_exact():
+    """The block-width autotuner runs each candidate width on the first calls of a
+    class of decompositions; every one of those calls is an exact SVD, and the
+    class ends up with a decision."""
+    q.set_autotune(True)
+    rng = np.random.default_rng(80)
+    t, blocks = _sector_tensor(rng, [(200, 180), (150, 150), (90, 60), (33, 31)])
+    for _ in range(5):
+        _check(t, blocks, _svd_with(t, "block", "tf32x3"), "tf32x3")
+    rep = q.autotune_report()
+    assert "fp32 R=8 " in rep and "tuned" in rep, rep

@@ -14,6 +14,8 @@ REQS = [serving.SolveRequest(i, L, delta, D, seed=100 + i)
 
 
 def test_results_same_alone_and_in_the_mix():
+    import quantit_gb300 as qq
+    qq.set_autotune(False)  # identical kernel choices alone and in the mix
     alone = serving.serial_solve_times(REQS, gemm="tf32x3", convergence=1e-8, max_sweeps=30)
     eng = serving.ServingEngine(slots=4, gemm="tf32x3", convergence=1e-8, max_sweeps=30)
     mixed = eng.run(REQS, realtime=False)
@@ -23,6 +25,7 @@ def test_results_same_alone_and_in_the_mix():
         # per-stream kernels are deterministic: the mix changes timing, not arithmetic
         assert r.energy == pytest.approx(E, rel=1e-12, abs=1e-12), (r.rid, r.energy, E)
         assert r.sweeps == sw
+    qq.set_autotune(True)
 
 
 def test_mixed_serving_energies_match_fp64_solves():
