@@ -9,7 +9,8 @@ full sweep (2(L-2) bond updates).  Synthetic data: no dataset is involved.
 Arms:
   (default)          our CUDA path through libqtt_gb300.so (qtt_dmrg); block GEMMs
                      in --mode (tf32x3 = split TF32 on tcgen05 tensor cores with an
-                     FP32 sector SVD -- the mixed path; f64 = the plain drop-in).
+                     FP32 sector SVD -- the mixed path; bf16x3 = the same with
+                     split-BF16 operands; f64 = the plain drop-in).
                      With --compare-f64 the plain FP64 path runs the same number of
                      sweeps from the same state; both final states are evaluated in
                      FP64 (<psi|H|psi>/<psi|psi>) for |dE| per site.
@@ -50,7 +51,7 @@ def parse():
                         "reached by a bond-dimension ramp)")
     p.add_argument("--L", type=int, default=None)
     p.add_argument("--D", type=int, default=None)
-    p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3"])
+    p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3", "bf16x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving", "contraction"],
@@ -251,6 +252,13 @@ def roofline(kind, st, P, mode, peaks_cache):
     sec = st["ms"] / 1e3
     base = {"kernel": kind, "per_launch_ms": st["ms"] / max(st["launches"], 1), "launches": st["launches"],
             "traffic": None}
+    if kind == "gemm" and mode == "bf16x3":
+        bf16 = P.get("bf16_tflops", 1939.7)
+        ach = st["work"] / sec / 1e12
+        return dict(base, bound="tensor", achieved=ach, peak=bf16, unit="TFLOP/s", frac=ach / bf16,
+                    tensor_ops_frac=6.0 * ach / bf16,
+                    peak_source="dense BF16 = MEASURED_PEAKS.json bf16_tflops (of measured); "
+                                "achieved counts useful FLOP, the split issues 6 tensor products each")
     if kind == "gemm" and mode != "f64":
         tf32 = P.get("bf16_tflops", 1939.7) / 2.0
         ach = st["work"] / sec / 1e12
@@ -301,14 +309,15 @@ def serving_section(q, args, full):
     from quantit_gb300 import serving
     dist = SERVING_FULL if full else SERVING_REDUCED
     reqs = serving.poisson_requests(args.serving_requests, rate=args.serving_rate, seed=0, **dist)
-    eng = serving.ServingEngine(slots=args.serving_slots, gemm=args.mode if args.mode != "f64" else "tf32x3",
+    mixed = args.mode if args.mode != "f64" else "tf32x3"
+    eng = serving.ServingEngine(slots=args.serving_slots, gemm=mixed,
                                 convergence=1e-8, max_sweeps=40, lanczos_steps=args.serving_lanczos)
     res = eng.run(reqs, realtime=True)
     mk = max(r.done for r in res) - min(r.arrival for r in res)
     out = serving.summarize([r.latency for r in res], mk, len(res))
     out.update({"requests": len(reqs), "rate_per_s": args.serving_rate, "slots": args.serving_slots,
                 "distribution": {"L": list(dist["lengths"]), "D": list(dist["bonds"]), "delta": [0.0, 2.0]},
-                "convergence": 1e-8, "gemm": "tf32x3", "lanczos_steps": args.serving_lanczos,
+                "convergence": 1e-8, "gemm": mixed, "lanczos_steps": args.serving_lanczos,
                 "peak_concurrency": eng.peak_concurrency,
                 "memory_budget_bytes": eng.memory_budget, "peak_admitted_bytes": eng.peak_memory,
                 "errors": sum(1 for r in res if r.error),
@@ -381,10 +390,6 @@ def contraction_workload(q, args):
     den = sum(float(np.sum(cf[k] ** 2)) for k in cf)
     nk = min(len(m["d"]), len(f["d"]))
     P = peaks()
-    g = m["kinds"]["gemm"]
-    per_launch = g["ms"] / max(g["launches"], 1) / 1e3
-    achieved = g["work"] / max(g["launches"], 1) / per_launch / 1e12 if g["launches"] else 0.0
-    tf32_peak = P.get("bf16_tflops", 1939.7) / 2.0
     return {"metric": "s per block-sparse contraction + sector-SVD truncation (theta pair at D)",
             "value": m["total_s"], "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": m["total_s"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -397,10 +402,7 @@ def contraction_workload(q, args):
             "speedup_vs_fp64": f["total_s"] / m["total_s"],
             "accuracy": {"C_rel_err": (num / den) ** 0.5, "d_max_rel_err": float(np.max(np.abs(m["d"][:nk] - f["d"][:nk])) / f["d"][0]),
                          "kept_mixed": m["kept"], "kept_fp64": f["kept"]},
-            "roofline_gemm": {"kernel": "gemm", "bound": "tensor", "achieved": achieved, "peak": tf32_peak,
-                              "unit": "TFLOP/s", "frac": achieved / tf32_peak, "traffic": None,
-                              "per_launch_ms": per_launch * 1e3, "launches": g["launches"],
-                              "peak_source": "dense TF32 = 1/2 of MEASURED_PEAKS.json bf16_tflops (of measured)"},
+            "roofline_gemm": roofline("gemm", m["kinds"]["gemm"], P, args.mode, {}),
             "kernel_time_ms": {k: v["ms"] for k, v in m["kinds"].items()}}
 
 
@@ -459,7 +461,8 @@ def main():
             print(json.dumps({"metric": "solves/s (XXZ ground states, Poisson arrivals) at p99 latency",
                               "value": sv["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": 1,
                               "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                              "dtype": "tf32x3+f32svd+f64", "data": "synthetic",
+                              "dtype": f"{args.mode if args.mode != 'f64' else 'tf32x3'}+f32svd+f64",
+                              "data": "synthetic",
                               "config": {"workload": "serving: Poisson stream of XXZ chain ground-state solves",
                                          "parallelism": "replicas only" if world > 1 else "single GPU"},
                               "serving": sv}))

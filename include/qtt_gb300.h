@@ -50,8 +50,10 @@ enum {
     QTT_ERR_NO_DATA = 9           /* structure-only btensor given to a numeric call */
 };
 enum { QTT_F64 = 0, QTT_F32 = 1 };
-/* precision of the block GEMMs (tensordot / matvec); SVD, inner products and the
- * 2x2 solve always run in FP64 */
+/* precision of the block GEMMs (tensordot / matvec): FP64, or split TF32 (hi/lo) or
+ * split BF16 (hi/mid/lo) on the tensor cores with FP32 accumulation.  Under a split
+ * mode the sector SVD / eigh run in FP32; inner products, norms and the 2x2 solve
+ * always run in FP64. */
 enum { QTT_GEMM_F64 = 0, QTT_GEMM_TF32X3 = 1, QTT_GEMM_BF16X3 = 2 };
 
 /* ------------------------------------------------------------------ library */

@@ -28,7 +28,7 @@ def _nvcc():
 def _compile(nvcc, src, verbose_ptxas=False):
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) > max(
-            os.path.getmtime(src), *[os.path.getmtime(os.path.join(CSRC, h)) for h in os.listdir(CSRC) if h.endswith(".h")],
+            os.path.getmtime(src), *[os.path.getmtime(os.path.join(CSRC, h)) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))],
             os.path.getmtime(os.path.join(HERE, "..", "include", "qtt_gb300.h"))):
         return obj, ""
     cmd = [nvcc, *ARCH, *FLAGS, "-c", src, "-o", obj]

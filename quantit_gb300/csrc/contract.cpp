@@ -266,9 +266,12 @@ int64_t prod_sizes(const BT &t, int64_t b, const std::vector<int64_t> &dims) {
 
 namespace {
 // Split every block of t (legs permuted by perm; the first nrow legs form the
-// rows, the rest the contracted K) into hi / lo TF32 arrays in matrix form.
+// rows, the rest the contracted K) into hi / lo TF32 arrays (TF32X3) or hi / mid / lo
+// BF16 arrays (BF16X3) in matrix form, rows zero padded to the mode's K granule.
 void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std::vector<int64_t> &offs, BufPtr &hi,
-                   BufPtr &lo, unsigned long long *amax) {
+                   BufPtr &mid, BufPtr &lo, unsigned long long *amax, int mode) {
+    const bool bf16 = mode == GEMM_BF16X3;
+    const int64_t gran = bf16 ? 8 : 4;
     const int r = t.rank;
     const int64_t nb = t.nblocks();
     offs.assign(nb, 0);
@@ -292,7 +295,7 @@ void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std:
             (i < nrow ? rows : K) *= shp[perm[i]];
         }
         if (K > INT32_MAX) fail(ERR_INVALID_ARGUMENT, "contracted dimension too large");
-        const int64_t K4 = (K + 3) & ~int64_t(3);
+        const int64_t K4 = (K + gran - 1) & ~(gran - 1);
         e.src_off = t.boff[b];
         e.dst_off = o;
         e.rank = r;
@@ -302,16 +305,24 @@ void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std:
         lens[b] = rows * K;
         o += rows * K4;
     }
-    const size_t bytes = size_t(std::max<int64_t>(o, 4)) * sizeof(float);
-    hi = dev_alloc(bytes);
-    lo = dev_alloc(bytes);
-    cuda_check(cudaMemsetAsync(hi->p, 0, bytes, ctx().stream), "cudaMemsetAsync(split)");
-    cuda_check(cudaMemsetAsync(lo->p, 0, bytes, ctx().stream), "cudaMemsetAsync(split)");
+    const size_t bytes = size_t(std::max<int64_t>(o, 8)) * (bf16 ? sizeof(uint16_t) : sizeof(float));
+    std::vector<BufPtr *> parts = {&hi, &lo};
+    if (bf16) parts.push_back(&mid);
+    for (BufPtr *b : parts) {
+        *b = dev_alloc(bytes);
+        cuda_check(cudaMemsetAsync((*b)->p, 0, bytes, ctx().stream), "cudaMemsetAsync(split)");
+    }
     auto chunks = make_chunks(lens);
-    StatScope sc(ST_PACK, 16.0 * double(std::accumulate(lens.begin(), lens.end(), int64_t(0))));
+    const double nel = double(std::accumulate(lens.begin(), lens.end(), int64_t(0)));
+    StatScope sc(ST_PACK, (bf16 ? 14.0 : 16.0) * nel);
     launch_amax(static_cast<const double *>(t.data()), t.nnz, amax);
-    launch_split_tf32(static_cast<const double *>(t.data()), static_cast<float *>(hi->p), static_cast<float *>(lo->p),
-                      upload_vec(ents), upload_vec(chunks), int64_t(chunks.size()), amax);
+    if (bf16)
+        launch_split_bf16x3(static_cast<const double *>(t.data()), hi->p, mid->p, lo->p, upload_vec(ents),
+                            upload_vec(chunks), int64_t(chunks.size()), amax);
+    else
+        launch_split_tf32(static_cast<const double *>(t.data()), static_cast<float *>(hi->p),
+                          static_cast<float *>(lo->p), upload_vec(ents), upload_vec(chunks), int64_t(chunks.size()),
+                          amax);
 }
 }  // namespace
 
@@ -324,7 +335,7 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
     const int mode = gemm_mode();
     const bool tc = mode != GEMM_F64;
     // operand buffers
-    BufPtr pa, pb, ahi, alo, bhi, blo, amax;
+    BufPtr pa, pb, ahi, amid, alo, bhi, bmid, blo, amax;
     std::vector<int64_t> offa, offb;
     const double *Ap = static_cast<const double *>(A.data());
     const double *Bp = static_cast<const double *>(B.data());
@@ -334,8 +345,8 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
         amax = dev_alloc(2 * sizeof(unsigned long long));
         cuda_check(cudaMemsetAsync(amax->p, 0, 2 * sizeof(unsigned long long), ctx().stream), "cudaMemsetAsync(amax)");
         auto *am = static_cast<unsigned long long *>(amax->p);
-        split_operand(A, P.p1, int(P.freeA.size()), offa, ahi, alo, am);
-        split_operand(B, P.p2p, int(P.freeB.size()), offb, bhi, blo, am + 1);
+        split_operand(A, P.p1, int(P.freeA.size()), offa, ahi, amid, alo, am, mode);
+        split_operand(B, P.p2p, int(P.freeB.size()), offb, bhi, bmid, blo, am + 1, mode);
         oa = &offa;
         ob = &offb;
     } else {
@@ -408,10 +419,12 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
         launch_gemm_f64(g);
     } else {
         TcArgs g;
-        g.Ahi = static_cast<const float *>(ahi->p);
-        g.Alo = static_cast<const float *>(alo->p);
-        g.Bhi = static_cast<const float *>(bhi->p);
-        g.Blo = static_cast<const float *>(blo->p);
+        g.Ahi = ahi->p;
+        g.Amid = amid ? amid->p : nullptr;
+        g.Alo = alo->p;
+        g.Bhi = bhi->p;
+        g.Bmid = bmid ? bmid->p : nullptr;
+        g.Blo = blo->p;
         g.amax_a = static_cast<const unsigned long long *>(amax->p);
         g.amax_b = g.amax_a + 1;
         g.C = static_cast<double *>(out.data());

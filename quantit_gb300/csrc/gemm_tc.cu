@@ -30,6 +30,7 @@
 
 #include "kernels.h"
 #include "qtt_core.h"
+#include "tc_common.cuh"
 
 namespace qtt {
 namespace {
@@ -42,109 +43,27 @@ constexpr int B_BYTES = TBN * TBK * 4;  // 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi/lo of A and B: 64 KB
 constexpr int NSTAGE = 3;
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024;
-constexpr uint32_t LBO = 128;                   // K-adjacent core matrices
-constexpr uint32_t SBO = (TBK * 4 / 16) * 128;  // next 8-row group: 1024 B
-constexpr long long WAIT_LIMIT = 1ll << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= uint64_t((saddr & 0x3FFFF) >> 4);
-    d |= uint64_t(LBO >> 4) << 16;
-    d |= uint64_t(SBO >> 4) << 32;
-    d |= uint64_t(1) << 46;  // descriptor version for tcgen05
-    return d;                // base offset 0, no swizzle (layout type 0)
-}
+using tc::LBO;
+using tc::SBO;
+using tc::smem_u32;
+using tc::make_desc;
+using tc::mbar_init;
+using tc::mbar_wait;
+using tc::amax_shift;
+using tc::f64_to_f32_int;
+using tc::f32_to_f64_int;
+using tc::st_shared_v4;
+static_assert(SBO == (TBK * 4 / 16) * 128, "the shared layout assumes 128-byte rows per K chunk");
 
 // kind::tf32, D=F32, A=B=TF32, both K-major, N=128, M=128
 __host__ __device__ constexpr uint32_t idesc_tf32() {
     return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(TBN >> 3) << 17) | (uint32_t(TBM >> 4) << 24);
 }
 
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    const uint32_t a = smem_u32(bar);
-    for (long long it = 0; it < WAIT_LIMIT; ++it) {
-        uint32_t ok;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return r;
-}
-
-// Exponent of an operand's max |x| (the scale 2^-shift brings it to [1, 2));
-// zero, infinite or NaN maxima leave the operand unscaled.
-__device__ __forceinline__ int amax_shift(unsigned long long bits) {
-    const int e = int((bits >> 52) & 0x7FF);
-    if (e == 0x7FF || bits == 0) return 0;
-    return (e == 0 ? 1 : e) - 1023;
-}
-
-// FP64 * 2^-shift -> FP32 (round to nearest, ties away) with integer operations only.
-// Magnitudes below the FP32 normal range flush to zero.
-__device__ __forceinline__ float f64_to_f32_int(double x, int shift) {
-    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
-    const uint32_t sign = uint32_t(b >> 63) << 31;
-    const int e = int((b >> 52) & 0x7FF);
-    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-    uint32_t f;
-    if (e == 0) {
-        f = 0;
-    } else if (e == 0x7FF) {
-        f = 0x7F800000u | (m ? 0x400000u : 0u);
-    } else {
-        const int fe = e - 1023 + 127 - shift;
-        if (fe <= 0) {
-            f = 0;
-        } else if (fe >= 255) {
-            f = 0x7F800000u;
-        } else {
-            const unsigned long long em = ((unsigned long long)fe << 52 | m) + (1ull << 28);
-            f = uint32_t(em >> 29);
-            if (f >= 0x7F800000u) f = 0x7F800000u;
-        }
-    }
-    return __uint_as_float(sign | f);
-}
-
-// FP32 * 2^shift -> FP64 (exact unless the result leaves the FP64 normal range,
-// where it flushes to zero or saturates to infinity) with integer operations only;
-// FP32 subnormals flush to zero.
-__device__ __forceinline__ double f32_to_f64_int(float f, int shift) {
-    const uint32_t b = __float_as_uint(f);
-    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
-    const uint32_t e = (b >> 23) & 0xFF, m = b & 0x7FFFFF;
-    unsigned long long d;
-    if (e == 0) {
-        d = sign;
-    } else if (e == 0xFF) {
-        d = sign | 0x7FF0000000000000ull | ((unsigned long long)m << 29);
-    } else {
-        const int de = int(e) - 127 + 1023 + shift;
-        if (de <= 0)
-            d = sign;
-        else if (de >= 0x7FF)
-            d = sign | 0x7FF0000000000000ull;
-        else
-            d = sign | ((unsigned long long)de << 52) | ((unsigned long long)m << 29);
-    }
-    return __longlong_as_double(static_cast<long long>(d));
 }
 
 __global__ void k_amax(const double *__restrict__ x, int64_t n, unsigned long long *amax) {
@@ -189,12 +108,6 @@ __global__ void k_split_tf32(const double *__restrict__ src, float *__restrict__
 // byte offset of (row r, k) in one operand copy of the canonical K-major layout
 __device__ __forceinline__ uint32_t kmaj_off(int r, int k) {
     return uint32_t(r >> 3) * SBO + uint32_t(k >> 2) * LBO + uint32_t(r & 7) * 16u + uint32_t(k & 3) * 4u;
-}
-
-__device__ __forceinline__ void st_shared_v4(char *p, uint4 v) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(smem_u32(p)), "r"(v.x), "r"(v.y), "r"(v.z),
-                 "r"(v.w)
-                 : "memory");
 }
 
 // rows x (TBK / 4) 16-byte vectors of one operand tile (hi and lo) into shared memory
@@ -276,8 +189,8 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
         const int K4 = (pr.K + 3) & ~3;
         char *st = smem + s * STAGE_BYTES;
         char *ahi = st, *alo = st + A_BYTES, *bhi = st + 2 * A_BYTES, *blo = st + 2 * A_BYTES + B_BYTES;
-        load_tile<TBM>(g.Ahi, g.Alo, pr.a_off, o.M, t.m0, K4, k0, ahi, alo, tid);
-        load_tile<TBN>(g.Bhi, g.Blo, pr.b_off, o.N, t.n0, K4, k0, bhi, blo, tid);
+        load_tile<TBM>(static_cast<const float *>(g.Ahi), static_cast<const float *>(g.Alo), pr.a_off, o.M, t.m0, K4, k0, ahi, alo, tid);
+        load_tile<TBN>(static_cast<const float *>(g.Bhi), static_cast<const float *>(g.Blo), pr.b_off, o.N, t.n0, K4, k0, bhi, blo, tid);
         k0 += TBK;
         // make the generic-proxy stores visible to the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -396,8 +309,13 @@ void launch_amax(const double *x, int64_t n, unsigned long long *amax) {
 }
 
 void launch_gemm_tc(const TcArgs &a, int mode) {
-    if (mode != GEMM_TF32X3) fail(ERR_INVALID_ARGUMENT, "this tensor-core GEMM precision mode is not built");
+    if (mode != GEMM_TF32X3 && mode != GEMM_BF16X3) fail(ERR_INVALID_ARGUMENT, "unknown tensor-core GEMM mode");
     if (a.ntiles <= 0) return;
+    if (mode == GEMM_BF16X3) {
+        launch_gemm_bf16x3(a, err_word(), ctx().stream);
+        ctx().tc_used = true;
+        return;
+    }
     static std::once_flag attr;
     std::call_once(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),

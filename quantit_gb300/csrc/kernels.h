@@ -69,7 +69,8 @@ void launch_gemm_f64(const GemmArgs &a);
 // Segment = one operand block; element e of the (rows x K) matrix reads
 // src[src_off + sum_d idx_d(e) * stride[d]] with idx(e) the row-major index over dims.
 struct SplitEntry {
-    int64_t src_off, dst_off;  // dst_off: element offset into hi / lo, multiple of 4
+    int64_t src_off, dst_off;  // dst_off: element offset into the split arrays, a multiple of the K granule
+    // K4: the padded row length (K rounded up to 4 for TF32X3, to 8 for BF16X3)
     int32_t rank, K, K4, pad;
     int64_t dims[8];
     int64_t stride[8];
@@ -82,9 +83,15 @@ void launch_split_tf32(const double *src, float *hi, float *lo, const SplitEntry
 // *amax (zeroed by the caller) <- max(*amax, bits of |x|) over n doubles (bit order =
 // value order for non-negative doubles, so the maximum is exact and deterministic).
 void launch_amax(const double *x, int64_t n, unsigned long long *amax);
-// A pair's a_off / b_off index the split arrays; A rows = M, B rows = N, K4 = (K + 3) & ~3.
+// Split-BF16 variant: hi / mid / lo bf16 (uint16) arrays in the same matrix form with
+// rows padded to K8 = (K + 7) & ~7 elements; the same amax scaling.
+void launch_split_bf16x3(const double *src, void *hi, void *mid, void *lo, const SplitEntry *e, const Chunk *chunks,
+                         int64_t nchunks, const unsigned long long *amax);
+// A pair's a_off / b_off index the split arrays; A rows = M, B rows = N.  Rows are padded
+// to K4 = (K + 3) & ~3 floats (TF32X3: hi / lo, mid unused) or K8 = (K + 7) & ~7 bf16
+// (BF16X3: hi / mid / lo).
 struct TcArgs {
-    const float *Ahi, *Alo, *Bhi, *Blo;
+    const void *Ahi, *Amid, *Alo, *Bhi, *Bmid, *Blo;
     const unsigned long long *amax_a, *amax_b;  // operand scales (see launch_split_tf32)
     double *C;
     const double *Cadd;
@@ -95,6 +102,8 @@ struct TcArgs {
     double alpha, beta;
 };
 void launch_gemm_tc(const TcArgs &a, int mode);
+// the BF16X3 kernel (called by launch_gemm_tc); err: the context's device error word
+void launch_gemm_bf16x3(const TcArgs &a, int *err, cudaStream_t stream);
 int gemm_tile_m(int mode);
 int gemm_tile_n(int mode);
 

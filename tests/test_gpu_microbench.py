@@ -34,11 +34,12 @@ def test_theta_pair_contraction_and_truncation_match_oracle(D):
         np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-12 * float(np.max(b)))
 
 
-def test_theta_pair_mixed_precision():
+@pytest.mark.parametrize("mode", ["tf32x3", "bf16x3"])
+def test_theta_pair_mixed_precision(mode):
     D = 96
     A, B = q.networks.theta_pair(D, seed=1)
     ref = dict(A.tensordot(B, ([2, 3], [1, 0])).blocks())
-    q.set_gemm_mode("tf32x3")
+    q.set_gemm_mode(mode)
     try:
         C = A.tensordot(B, ([2, 3], [1, 0]))
         U, d, V = q.linalg.svd(C, 2, 1e-10, min_size=1, max_size=D)

@@ -1,6 +1,7 @@
-"""The split-TF32 tcgen05 grouped GEMM (pytest -m gpu).
+"""The split-precision tcgen05 grouped GEMMs (pytest -m gpu).
 
-Tolerance: TF32x3 keeps hi*hi + hi*lo + lo*hi with FP32 accumulation, about FP32
+Tolerance: TF32x3 keeps hi*hi + hi*lo + lo*hi, BF16x3 the six products of order <= 2
+of the hi / mid / lo bf16 terms; both accumulate in FP32 and reach about FP32
 accuracy, so a block product agrees with the FP64 result to 2e-6 relative to the
 block's largest magnitude (checked against the oracle)."""
 import numpy as np
@@ -15,10 +16,13 @@ pytestmark = pytest.mark.gpu
 TOL = 2e-6
 
 
-@pytest.fixture
-def tf32x3():
-    q.set_gemm_mode("tf32x3")
-    yield
+TC_MODES = ("tf32x3", "bf16x3")
+
+
+@pytest.fixture(params=TC_MODES)
+def tc_mode(request):
+    q.set_gemm_mode(request.param)
+    yield request.param
     q.set_gemm_mode("f64")
 
 
@@ -32,7 +36,7 @@ def _check(got, want, tol=TOL):
         assert err <= tol * scale, (k, err, scale)
 
 
-def test_tc_gemm_random_layouts(tf32x3):
+def test_tc_gemm_random_layouts(tc_mode):
     rng = np.random.default_rng(21)
     n = 0
     for trial in range(600):
@@ -49,7 +53,7 @@ def test_tc_gemm_random_layouts(tf32x3):
 
 
 @pytest.mark.parametrize("sizes", [(40, 70, 33), (130, 257, 129), (300, 190, 200)])
-def test_tc_gemm_large_blocks(tf32x3, sizes):
+def test_tc_gemm_large_blocks(tc_mode, sizes):
     a, b, c = sizes
     rng = np.random.default_rng(22)
     A = o.btensor([[(a, -1), (b, 0), (c, 1)], [(1, -1), (1, 1)], [(1, -1), (1, 1)], [(c, -2), (b, 0), (a, 2)]],
@@ -65,7 +69,7 @@ def test_tc_gemm_large_blocks(tf32x3, sizes):
         _check(to_device(A).tensordot(to_device(B), (dA, dB)), want, tol=5e-6)
 
 
-def test_tc_gemm_tensorgdot_epilogue(tf32x3):
+def test_tc_gemm_tensorgdot_epilogue(tc_mode):
     rng = np.random.default_rng(23)
     A, B, dA, dB = _contractible_pair(rng, (0,), 3, 3, 1)
     while not A.blocks or not B.blocks:
@@ -77,7 +81,7 @@ def test_tc_gemm_tensorgdot_epilogue(tf32x3):
 
 
 def test_mixed_dmrg_energy_close_to_fp64():
-    """Converged runs: the mixed path (split-TF32 block GEMMs, FP32 sector SVD)
+    """Converged runs: the mixed paths (split-TF32 or split-BF16 block GEMMs, FP32 sector SVD)
     reports the FP64 variational energy of its final state, which matches the
     plain FP64 path to better than 1e-8 per site.  (Its per-bond Ritz values carry
     ~1e-6 relative noise from FP32 accumulation and are not used for the result.)"""
@@ -86,20 +90,21 @@ def test_mixed_dmrg_energy_close_to_fp64():
         mps = o.right_canonicalize(o.random_mps(L, D, [1, -1], 0, np.random.default_rng(5)))
         dmpo = q.networks.bMPO([to_device(t) for t in mpo])
         res = {}
-        for mode in ("f64", "tf32x3"):
+        for mode in ("f64",) + TC_MODES:
             dmps = q.networks.bMPS([to_device(t) for t in mps], 0)
             res[mode] = q.algorithms.dmrg(dmpo, dmps, q.algorithms.dmrg_options(
                 cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4, maximum_iterations=sweeps,
                 gemm=mode))
             e, n2 = q.algorithms.mps_energy(dmpo, dmps)
             assert abs(n2 - 1.0) < 1e-5
-            if mode == "tf32x3":
+            if mode != "f64":
                 assert res[mode] == pytest.approx(e / n2, rel=1e-14)
-        assert abs(res["tf32x3"] - res["f64"]) / L < 1e-8, (L, D, res)
+        for mode in TC_MODES:
+            assert abs(res[mode] - res["f64"]) / L < 1e-8, (L, D, mode, res)
 
 
 @pytest.mark.parametrize("scale_a, scale_b", [(1e-60, 1.0), (1e-30, 1e-30), (1e45, 1e-40), (3e-200, 2e150)])
-def test_tc_gemm_operand_magnitudes(tf32x3, scale_a, scale_b):
+def test_tc_gemm_operand_magnitudes(tc_mode, scale_a, scale_b):
     # operands far outside the FP32 range: each is scaled by an exact power of two
     # before the split and the product is scaled back in the epilogue
     rng = np.random.default_rng(24)
@@ -118,10 +123,11 @@ def test_mixed_dmrg_from_noncanonical_state():
     L, D = 32, 48
     mpo = q.networks.xxz(L, 1.0)
     out = {}
-    for gemm in ("f64", "tf32x3"):
+    for gemm in ("f64",) + TC_MODES:
         mps = q.networks.random_bmps(L, D, seed=5)
         opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=1e-9, max_bond=D, min_bond=1,
                                          maximum_iterations=20, gemm=gemm, final_energy_fp64=True)
         out[gemm] = q.algorithms.dmrg(mpo, mps, opts)
-    assert np.isfinite(out["tf32x3"])
-    assert abs(out["tf32x3"] - out["f64"]) / L < 1e-7, out
+    for gemm in TC_MODES:
+        assert np.isfinite(out[gemm])
+        assert abs(out[gemm] - out["f64"]) / L < 1e-7, (gemm, out)
