@@ -164,17 +164,19 @@ struct JacobiParams {
     int64_t max_steps;
     int *sweeps;   // per sector (written at the end)
     int *rotated;  // nsec * max_sweeps flags, zero on entry: a rotation happened in (sector, sweep)
+    const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
 };
 
 // Rotation of one column pair by one warp.  With R > 0 (p <= 32 R) every lane
 // first loads its R elements of both columns into registers -- one round trip to
 // L2 instead of one per element -- then forms the three inner products, the
 // rotation, and writes back from registers; the rotation-matrix columns follow
-// the same pattern.  R == 0 streams columns of any length.  Returns whether a
-// rotation was applied.
+// the same pattern.  R == 0 streams columns of any length.  A nonzero column whose
+// squared norm is at most thr (> 0) is deflated: set to zero, never rotated again.
+// Returns whether a column was rotated or deflated.
 template <class T, int R>
 __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ wb, T *__restrict__ va,
-                                            T *__restrict__ vb, int p, int q, int lane) {
+                                            T *__restrict__ vb, int p, int q, int lane, T thr) {
     T al = 0, be = 0, ga = 0;
     T x[R > 0 ? R : 1], y[R > 0 ? R : 1];
     if (R > 0) {
@@ -201,6 +203,14 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
     al = wsum(al);
     be = wsum(be);
     ga = wsum(ga);
+    const bool za = thr > T(0) && al > T(0) && al <= thr, zb = thr > T(0) && be > T(0) && be <= thr;
+    if (za || zb) {
+        for (int r = lane; r < p; r += 32) {
+            if (za) wa[r] = T(0);
+            if (zb) wb[r] = T(0);
+        }
+        return true;
+    }
     if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
     T sn, tau;
     rot_params(al, be, ga, sn, tau);
@@ -308,7 +318,7 @@ __global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
             T *wb = P.work + sd.w_off + int64_t(b) * sd.p;
             T *va = P.rot + sd.rot_off + int64_t(a) * sd.q;
             T *vb = P.rot + sd.rot_off + int64_t(b) * sd.q;
-            if (!rotate_pair<T, R>(wa, wb, va, vb, sd.p, sd.q, lane)) continue;
+            if (!rotate_pair<T, R>(wa, wb, va, vb, sd.p, sd.q, lane, P.defl ? P.defl[s] : T(0))) continue;
             if (lane == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
         }
         grid.sync();
@@ -365,6 +375,7 @@ struct BJacobiParams {
     int max_jobs;  // >= block pairs per step
     int upj;       // V work units (row chunks of one CTA width) per job
     int max_q;     // widest sector (columns)
+    const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
 };
 
 __device__ __forceinline__ int bj_items(int q, int B) {
@@ -409,12 +420,21 @@ __device__ __forceinline__ void bj_store(const T (&x)[R], T *slot, int lane) {
     }
 }
 
+// Per-lane partial sums in NA independent chains (the dot product is on the
+// critical path of every round: R dependent FMAs would cost R FMA latencies).
 template <class T, int R>
 __device__ __forceinline__ T bj_dot(const T (&x)[R], const T (&y)[R]) {
-    T a = 0;
+    constexpr int NA = R >= 16 ? 4 : (R >= 4 ? 2 : 1);
+    T a[NA];
 #pragma unroll
-    for (int i = 0; i < R; ++i) a = fma(x[i], y[i], a);
-    return wsum(a);
+    for (int k = 0; k < NA; ++k) a[k] = T(0);
+#pragma unroll
+    for (int i = 0; i < R; ++i) a[i % NA] = fma(x[i], y[i], a[i % NA]);
+#pragma unroll
+    for (int w = NA / 2; w > 0; w >>= 1)
+#pragma unroll
+        for (int k = 0; k < w; ++k) a[k] += a[k + w];
+    return wsum(a[0]);
 }
 
 // Rotation parameters from the multi-function unit (FP32 only).  t need not be
@@ -443,8 +463,12 @@ __device__ __forceinline__ void bj_params_fast(float al, float be, float ga, flo
 // from al' = al - t ga, be' = be + t ga (t = tan theta), and are recomputed from
 // the columns when that update cancels (norm drops below 1/16).  Same acceptance
 // test and rotation as rotate_pair (tol = Eps<T>::tol(p), hoisted by the caller).
+// A zero column (norm 0) is skipped without forming the product; with thr > 0 a
+// column whose squared norm falls to thr or below after the rotation is deflated
+// (set to zero, norm 0).
 template <class T, int R>
-__device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T &sn, T &tau) {
+__device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T thr, T &sn, T &tau) {
+    if (al == T(0) || be == T(0)) return false;
     const T ga = bj_dot(x, y);
     if (ga == T(0)) return false;
     T t;
@@ -460,30 +484,42 @@ __device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T 
     const T a2 = al - t * ga, b2 = be + t * ga;
     al = (a2 > al * T(0.0625)) ? a2 : bj_dot(x, x);
     be = (b2 > be * T(0.0625)) ? b2 : bj_dot(y, y);
+    if (thr > T(0)) {
+        if (al <= thr) {
+#pragma unroll
+            for (int i = 0; i < R; ++i) x[i] = T(0);
+            al = T(0);
+        }
+        if (be <= thr) {
+#pragma unroll
+            for (int i = 0; i < R; ++i) y[i] = T(0);
+            be = T(0);
+        }
+    }
     return true;
 }
 
 template <class T, int NP>
 __device__ __forceinline__ T bj_qdot(const T (&vr)[NP], const T *qcol) {
-    T acc = 0;
+    T acc0 = 0, acc1 = 0;
     if constexpr (sizeof(T) == 4) {
 #pragma unroll
         for (int j = 0; j < NP / 4; ++j) {
             const float4 qv = reinterpret_cast<const float4 *>(qcol)[j];
-            acc = fma(vr[4 * j], qv.x, acc);
-            acc = fma(vr[4 * j + 1], qv.y, acc);
-            acc = fma(vr[4 * j + 2], qv.z, acc);
-            acc = fma(vr[4 * j + 3], qv.w, acc);
+            acc0 = fma(vr[4 * j], qv.x, acc0);
+            acc1 = fma(vr[4 * j + 1], qv.y, acc1);
+            acc0 = fma(vr[4 * j + 2], qv.z, acc0);
+            acc1 = fma(vr[4 * j + 3], qv.w, acc1);
         }
     } else {
 #pragma unroll
         for (int j = 0; j < NP / 2; ++j) {
             const double2 qv = reinterpret_cast<const double2 *>(qcol)[j];
-            acc = fma(vr[2 * j], qv.x, acc);
-            acc = fma(vr[2 * j + 1], qv.y, acc);
+            acc0 = fma(vr[2 * j], qv.x, acc0);
+            acc1 = fma(vr[2 * j + 1], qv.y, acc1);
         }
     }
-    return acc;
+    return acc0 + acc1;
 }
 
 // V[r, cols] <- V[r, cols] Q for rows [r0, r1) of the 2B columns of blocks a and b
@@ -623,6 +659,8 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             T *W = P.work + sd.w_off;
             T *V = P.rot + sd.rot_off;
             const T tol = Eps<T>::tol(p);
+            const T thr = P.defl ? P.defl[s] : T(0);
+            bool zeroed = false;
 
             for (int j = warp; j < NP; j += B) {
                 if (!valid(j)) continue;
@@ -641,12 +679,19 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     cols[j * PP + lane + 32 * i] = v[i];
                 }
                 acc = wsum(acc);
+                if (thr > T(0) && acc > T(0) && acc <= thr) {
+                    // a numerically zero column: deflated (zero from here on)
+#pragma unroll
+                    for (int i = 0; i < R; ++i) cols[j * PP + lane + 32 * i] = T(0);
+                    acc = T(0);
+                    zeroed = true;
+                }
                 if (lane == 0) nrm[j] = acc;
             }
             for (int e = tid; e < NP * NP; e += NT) Qs[e] = (e % (NP + 1) == 0) ? T(1) : T(0);
             if (tid == 0) any_rot = 0;
             __syncthreads();
-            bool rotated_any = false;
+            bool rotated_any = zeroed;
             T x[R], y[R], sn, tau;
             if (k == 0) {
                 // intra-block pairs: round-robin over the B columns of each block
@@ -660,7 +705,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                         bj_load(x, cols + u * PP, lane);
                         bj_load(y, cols + v * PP, lane);
                         T al = nrm[u], be = nrm[v];
-                        if (bj_rotate(x, y, al, be, tol, sn, tau)) {
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau)) {
                             bj_store(x, cols + u * PP, lane);
                             bj_store(y, cols + v * PP, lane);
                             if (lane < NP) {
@@ -694,7 +739,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     if (mine && valid(j)) {
                         bj_load(y, cols + j * PP, lane);
                         T be = nrm[j];
-                        if (bj_rotate(x, y, al, be, tol, sn, tau)) {
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau)) {
                             bj_store(y, cols + j * PP, lane);
                             if (lane < NP) {
                                 T qy = Qs[j * NP + lane];
@@ -772,13 +817,38 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
         for (int s = tid; s < nsec; s += NT) P.sweeps[s] = sweep[s];
 }
 
+// Deflation thresholds of the SVD sectors: thr[s] = delta2 * ||W_s||_F^2, summed in
+// a fixed order (the value, and so every deflation decision, is deterministic);
+// 0 for eigh sectors.
+template <class T>
+__global__ void __launch_bounds__(256) k_defl_thr(const T *__restrict__ work, const SectorDesc *__restrict__ secs,
+                                                  double delta2, T *__restrict__ thr) {
+    __shared__ double red[8];
+    const SectorDesc sd = secs[blockIdx.x];
+    const int64_t n = int64_t(sd.p) * sd.q;
+    const T *W = work + sd.w_off;
+    double acc = 0.0;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+        const double x = double(W[e]);
+        acc = fma(x, x, acc);
+    }
+    acc = wsum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < 8; ++i) t += red[i];
+        thr[blockIdx.x] = sd.mode == 0 ? T(delta2 * t) : T(0);
+    }
+}
+
 // One CTA per sector: column norms, ordering, normalisation, completion.
 // scratch: at least p doubles per sector at offset w_off (the candidate vector).
 template <class T>
 __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, const T *__restrict__ rot,
                                                  double *__restrict__ U, double *__restrict__ V,
                                                  double *__restrict__ S, const SectorDesc *__restrict__ secs,
-                                                 double *__restrict__ scratch) {
+                                                 double *__restrict__ scratch, int cap) {
     extern __shared__ double sh[];
     const SectorDesc sd = secs[blockIdx.x];
     const int q = sd.q, p = sd.p;
@@ -837,8 +907,11 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
     __shared__ double bcast;
     __shared__ int accepted;
     double *cand = scratch + sd.w_off;
+    int completed = 0;
     for (int jz = 0; jz < q; ++jz) {
         if (sig[perm[jz]] > 0.0) continue;
+        if (cap >= 0 && completed >= cap) break;  // the rest are truncated away by the caller
+        ++completed;
         for (int e = 0; e < p; ++e) {
             for (int r = threadIdx.x; r < p; r += blockDim.x) cand[r] = (r == e) ? 1.0 : 0.0;
             __syncthreads();
@@ -1076,7 +1149,7 @@ void tune_save(const TuneKey &k, int w) {
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
                  int max_sweeps, int *sweeps_out, int *flags, int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes,
-                 cudaStream_t stream) {
+                 const T *defl, cudaStream_t stream) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
@@ -1090,6 +1163,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
         B.max_steps = 0;
         B.sweeps = sweeps_out;
         B.rotated = flags;
+        B.defl = defl;
         B.max_q = max_steps_per_sweep + 1;  // the widest sector's even column count bounds q
         const bool f32 = sizeof(T) == 4;
         const std::vector<int> cands = block_widths(f32, r_class(max_p));
@@ -1146,6 +1220,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     P.max_steps = int64_t(max_sweeps) * std::max(1, max_steps_per_sweep) + 1;
     P.sweeps = sweeps_out;
     P.rotated = flags;
+    P.defl = defl;
     const int64_t pairs = (sum_q + nsec) / 2 + nsec;  // pairs per step, an upper bound
     // registers per lane: the longest column over the sectors decides
     if (max_p <= 4 * 32)
@@ -1162,7 +1237,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
 
 template <class T>
 void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
-                 int max_q, double *scratch, cudaStream_t stream) {
+                 int max_q, double *scratch, int cap, cudaStream_t stream) {
     size_t smem = size_t(max_q) * (sizeof(double) + sizeof(int)) + 16;
     static std::once_flag attr;
     std::call_once(attr, [] {
@@ -1170,7 +1245,7 @@ void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, c
                    "finish smem attribute");
     });
     if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the SVD finishing kernel");
-    k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch);
+    k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch, cap);
     count_launch();
     cuda_check(cudaGetLastError(), "SVD finishing kernel launch");
 }
@@ -1199,21 +1274,35 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes) {
+                      int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl) {
     if (nsec <= 0) return;
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
-                    max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes, stream);
+                    max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
+                    static_cast<const float *>(defl), stream);
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
-                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes, stream);
+                    max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
+                    static_cast<const double *>(defl), stream);
 }
 
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
-                   int64_t sum_q, void *vwork, size_t vwork_bytes) {
+                   int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl) {
     launch_jacobi_on(ctx().stream, work, rot, sec, slot_start, nsec, max_steps_per_sweep, max_sweeps, sweeps_out, flags,
-                     f32, max_p, sum_q, vwork, vwork_bytes);
+                     f32, max_p, sum_q, vwork, vwork_bytes, defl);
+}
+
+void launch_deflation_thresholds(const void *work, const SectorDesc *sec, int nsec, double delta, void *thr, int f32) {
+    if (nsec <= 0) return;
+    if (f32)
+        k_defl_thr<float><<<nsec, 256, 0, ctx().stream>>>(static_cast<const float *>(work), sec, delta * delta,
+                                                          static_cast<float *>(thr));
+    else
+        k_defl_thr<double><<<nsec, 256, 0, ctx().stream>>>(static_cast<const double *>(work), sec, delta * delta,
+                                                           static_cast<double *>(thr));
+    count_launch();
+    cuda_check(cudaGetLastError(), "deflation threshold kernel launch");
 }
 
 size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int max_sweeps, int f32) {
@@ -1228,19 +1317,19 @@ size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int 
 }
 
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
-                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32) {
+                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap) {
     if (nsec <= 0) return;
     if (f32)
         finish_impl(static_cast<const float *>(work), static_cast<const float *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch, stream);
+                    scratch, complete_cap, stream);
     else
         finish_impl(static_cast<const double *>(work), static_cast<const double *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch, stream);
+                    scratch, complete_cap, stream);
 }
 
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
-                   int max_q, double *scratch, int f32) {
-    launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32);
+                   int max_q, double *scratch, int f32, int complete_cap) {
+    launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32, complete_cap);
 }
 
 }  // namespace qtt

@@ -174,22 +174,30 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 // vwork (optional, jacobi_vwork_bytes): lets the block kernel defer each step's V
 // updates to the next step, where CTAs without a block pair run them; without it
 // every CTA updates V right after its block pair.
+// defl (optional, launch_deflation_thresholds, the work type): per sector, a column
+// whose squared norm falls to the threshold or below is set to zero and leaves the
+// sweeps (a numerically zero column); null: no deflation.
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
-                   int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0);
+                   int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0, const void *defl = nullptr);
+// thr[s] <- delta^2 ||W_s||_F^2 for every svd sector (0 for eigh), in the work type.
+void launch_deflation_thresholds(const void *work, const SectorDesc *sec, int nsec, double delta, void *thr, int f32);
 size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int max_sweeps, int f32);
 // Column norms, sort (descending for svd, ascending eigenvalues for eigh),
 // normalisation and completion of null columns; writes U (m x k), V (n x k)
 // column-major and s (k) per sector in FP64, k = min(m, n).  max_q: largest q;
-// scratch: FP64 buffer with the work buffer's element offsets.
+// scratch: FP64 buffer with the work buffer's element offsets.  complete_cap >= 0
+// completes only the first complete_cap null columns of each sector (in value
+// order): the caller truncates the others away.
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec,
-                   int nsec, int max_q, double *scratch, int f32);
+                   int nsec, int max_q, double *scratch, int f32, int complete_cap = -1);
 // The same two launches on an explicit stream (no library context involved).
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p, int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0);
+                      int max_p, int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0,
+                      const void *defl = nullptr);
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
-                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32);
+                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap = -1);
 // Segment = one output block (rows x k row-major at dst_off) from a column-major
 // (ld x *) sector matrix at src_off: dst[i*k + j] = src[src_off + (r0 + i) + j*ld].
 struct ScatterEntry {

@@ -147,6 +147,26 @@ LastSweeps &last_sweeps() {
     return l;
 }
 
+// Set by svd_truncated around the decomposition it runs: its caller keeps only the
+// values the truncation selects, at least min_size of them.  An FP32 sector SVD then
+// deflates numerically zero columns (norm <= FP32 epsilon x the sector's Frobenius
+// norm, below what FP32 arithmetic resolves): they become exact zeros, which the
+// truncation discards, and only min_size null columns per sector need completing.
+struct TruncHint {
+    bool active = false;
+    int64_t min_size = 0;
+};
+TruncHint &trunc_hint() {
+    thread_local TruncHint h;
+    return h;
+}
+struct ScopedTruncHint {
+    TruncHint saved;
+    ScopedTruncHint(bool on, int64_t min_size) : saved(trunc_hint()) { trunc_hint() = TruncHint{on, min_size}; }
+    ~ScopedTruncHint() { trunc_hint() = saved; }
+};
+constexpr double kDeflateF32 = 1.1920928955078125e-07;  // FP32 epsilon (2^-23)
+
 struct Decomp {
     std::vector<Sector> secs;
     std::vector<SectorDesc> desc;  // one per (sector, batch element)
@@ -264,10 +284,17 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
         StatScope sc(ST_SVD, 0.0);
         const size_t vb = jacobi_vwork_bytes(nsec, stot, max_steps, max_sweeps, f32);
         BufPtr vwork = dev_alloc(vb);
+        BufPtr thr;
+        int cap = -1;
+        if (mode == 0 && f32 && trunc_hint().active) {
+            thr = dev_alloc(size_t(nsec) * es);
+            launch_deflation_thresholds(W, dsec, nsec, kDeflateF32, thr->p, f32);
+            cap = int(std::min<int64_t>(std::max<int64_t>(trunc_hint().min_size, 0), INT32_MAX));
+        }
         launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
-                      vwork->p, vb);
+                      vwork->p, vb, thr ? thr->p : nullptr);
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
-                      static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32);
+                      static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32, cap);
     }
 }
 
@@ -577,7 +604,12 @@ SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, dou
 }
 
 SVDOut svd_truncated(const BT &t, int64_t split, double tol, int64_t min_size, int64_t max_size, double pw) {
-    return truncate(svd_split(t, split), max_size, min_size, tol, pw, true);
+    SVDOut full;
+    {
+        ScopedTruncHint hint(tol > 0.0, min_size);
+        full = svd_split(t, split);
+    }
+    return truncate(std::move(full), max_size, min_size, tol, pw, true);
 }
 
 // eigh(btensor, upper), btensor_linalg.cpp:294-368 (eigenvalues ascending per sector)

@@ -110,3 +110,90 @@ def test_autotuner_times_both_widths_and_results_stay_exact():
         _check(t, blocks, _svd_with(t, "block", "tf32x3"), "tf32x3")
     rep = q.autotune_report()
     assert "fp32 R=8 " in rep and "tuned" in rep, rep
+
+
+def _last_sweeps():
+    import ctypes as C
+    buf = (C.c_int32 * 4096)()
+    n = C.c_int32()
+    assert q.lib().qtt_last_svd_sweeps(buf, 4096, C.byref(n)) == 0
+    return list(buf[:n.value])
+
+
+def _low_rank_tensor(rng, shapes, ranks):
+    blocks = []
+    for i, ((m, n), r) in enumerate(zip(shapes, ranks)):
+        k = min(m, n)
+        # r resolved values over five decades, the rest far below FP32 resolution
+        s = np.concatenate([np.logspace(0, -5, r), 1e-10 * rng.uniform(size=k - r)])
+        u, _ = np.linalg.qr(rng.standard_normal((m, k)))
+        v, _ = np.linalg.qr(rng.standard_normal((n, k)))
+        blocks.append(((i, i), (u * s) @ v.T))
+    legs = [[(m, Z(i)) for i, (m, _) in enumerate(shapes)], [(n, Z(-i)) for i, (_, n) in enumerate(shapes)]]
+    t = q.btensor(legs, Z(0))
+    t.set_blocks(blocks)
+    return t, blocks
+
+
+def _isometry_error(F):
+    """max |F^H F - I| over the new (last) leg's sectors of a factor."""
+    cols = {}
+    for k, b in F.blocks():
+        cols.setdefault(k[-1], []).append(b.reshape(-1, b.shape[-1]))
+    err = 0.0
+    for v in cols.values():
+        m = np.concatenate(v, axis=0)
+        err = max(err, float(np.max(np.abs(m.T @ m - np.eye(m.shape[1])))))
+    return err
+
+
+@pytest.mark.parametrize("kernel", ["block", "scalar"])
+def test_truncated_fp32_svd_deflates_unresolved_columns(kernel):
+    """svd with a cutoff on the mixed path: columns whose norm falls below FP32
+    epsilon x their sector's Frobenius norm are deflated to exact zeros and leave
+    the sweeps; the truncation discards them.  The resolved values match LAPACK to
+    FP32 accuracy and the kept factors are isometries."""
+    rng = np.random.default_rng(81)
+    shapes, ranks = [(150, 130), (90, 80), (40, 40), (12, 9)], [30, 20, 10, 9]
+    t, blocks = _low_rank_tensor(rng, shapes, ranks)
+    q.set_autotune(False)
+    q.set_jacobi_kernel(kernel)
+    q.set_gemm_mode("tf32x3")
+    try:
+        q.linalg.svd(t)
+        full_sweeps = _last_sweeps()
+        U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=1, max_size=10 ** 6)
+        defl_sweeps = _last_sweeps()
+    finally:
+        q.set_jacobi_kernel("block")
+        q.set_gemm_mode("f64")
+        q.set_autotune(True)
+    assert max(defl_sweeps) <= max(full_sweeps), (defl_sweeps, full_sweeps)
+    new_section = {k[0]: k[1] for k, _ in U.blocks()}
+    dv = dict(d.blocks())
+    for i, ((_, a), r) in enumerate(zip(blocks, ranks)):
+        want = np.linalg.svd(a, compute_uv=False)
+        got = dv[(new_section[i],)]
+        assert len(got) >= r
+        np.testing.assert_allclose(got[:r], want[:r], atol=4 * 3e-6 * want[0], rtol=0)
+        assert np.all(got[r:] < 1e-6 * want[0])  # unresolved values that did not deflate
+    assert _isometry_error(U) < 1e-5
+    assert _isometry_error(V) < 1e-5
+    R = dict(U.mul(d).tensordot(V.conj(), ([1], [1])).blocks())
+    for k, a in blocks:
+        np.testing.assert_allclose(R[k], a, atol=1e-5 * float(np.max(np.abs(a))), rtol=0)
+
+
+def test_truncated_fp32_svd_completes_null_columns_up_to_min_size():
+    """min_size above the numerical rank keeps zero singular values: their left
+    vectors are completed to an orthonormal set, so U stays an isometry."""
+    rng = np.random.default_rng(82)
+    t, blocks = _low_rank_tensor(rng, [(30, 24)], [2])
+    q.set_gemm_mode("tf32x3")
+    try:
+        U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=6, max_size=10 ** 6)
+    finally:
+        q.set_gemm_mode("f64")
+    assert sum(d.section_sizes) == 6
+    assert _isometry_error(U) < 1e-5
+    assert _isometry_error(V) < 1e-5
