@@ -25,6 +25,13 @@ def set_autotune(on):
     call("qtt_set_autotune", 1 if on else 0)
 
 
+def set_svd_deflation(on):
+    """Deflate columns below FP32 resolution in the mixed path's truncating SVDs
+    (on by default)."""
+    from ._lib import call
+    call("qtt_set_svd_deflation", 1 if on else 0)
+
+
 def autotune_report():
     """The autotuner's decisions, one line per class of decomposition."""
     import ctypes as C

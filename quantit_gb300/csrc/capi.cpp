@@ -96,6 +96,9 @@ int qtt_device_memory(int64_t *free_bytes, int64_t *total_bytes) {
 int qtt_set_autotune(int on) {
     return guarded([&] { qtt::set_autotune(on); });
 }
+int qtt_set_svd_deflation(int on) {
+    return guarded([&] { qtt::set_svd_deflation(on); });
+}
 int qtt_autotune_report(char *buf, int64_t cap, int64_t *len) {
     return guarded([&] {
         const std::string r = qtt::autotune_report();

@@ -148,10 +148,11 @@ LastSweeps &last_sweeps() {
 }
 
 // Set by svd_truncated around the decomposition it runs: its caller keeps only the
-// values the truncation selects, at least min_size of them.  An FP32 sector SVD then
-// deflates numerically zero columns (norm <= FP32 epsilon x the sector's Frobenius
-// norm, below what FP32 arithmetic resolves): they become exact zeros, which the
-// truncation discards, and only min_size null columns per sector need completing.
+// values the truncation selects, and the truncation never keeps a zero value
+// (btensor_linalg.cpp:658-755 keeps values strictly above the smallest kept one
+// less 2 eps, which is >= 0).  So null columns need no completion, and an FP32
+// sector SVD deflates numerically zero columns (norm <= FP32 epsilon x the sector's
+// Frobenius norm, below what FP32 arithmetic resolves) to exact zeros.
 struct TruncHint {
     bool active = false;
     int64_t min_size = 0;
@@ -285,11 +286,12 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
         const size_t vb = jacobi_vwork_bytes(nsec, stot, max_steps, max_sweeps, f32);
         BufPtr vwork = dev_alloc(vb);
         BufPtr thr;
-        int cap = -1;
-        if (mode == 0 && f32 && trunc_hint().active) {
+        // a truncation keeps only values above its (non-negative) threshold, never a
+        // zero one: null columns need no completion under a truncating svd
+        const int cap = (mode == 0 && trunc_hint().active) ? 0 : -1;
+        if (mode == 0 && f32 && trunc_hint().active && svd_deflation()) {
             thr = dev_alloc(size_t(nsec) * es);
             launch_deflation_thresholds(W, dsec, nsec, kDeflateF32, thr->p, f32);
-            cap = int(std::min<int64_t>(std::max<int64_t>(trunc_hint().min_size, 0), INT32_MAX));
         }
         launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
                       vwork->p, vb, thr ? thr->p : nullptr);

@@ -314,6 +314,9 @@ int jacobi_variant();
 // Block-width autotuner of the block-Jacobi kernel (on by default) and its decisions.
 void set_autotune(int on);
 std::string autotune_report();
+// Deflation of numerically zero columns in the FP32 SVD of a truncating svd (on by default).
+void set_svd_deflation(int on);
+int svd_deflation();
 // Non-zero when a tensor-core kernel gave up on a bounded wait since the last
 // check (synchronises the device; read and cleared).
 int tc_error_check();

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import quantit_gb300 as q
+from oracle import qtt_oracle as o
 from quantit_gb300.conserved import Z
 
 pytestmark = pytest.mark.gpu
@@ -184,9 +185,10 @@ def test_truncated_fp32_svd_deflates_unresolved_columns(kernel):
         np.testing.assert_allclose(R[k], a, atol=1e-5 * float(np.max(np.abs(a))), rtol=0)
 
 
-def test_truncated_fp32_svd_completes_null_columns_up_to_min_size():
-    """min_size above the numerical rank keeps zero singular values: their left
-    vectors are completed to an orthonormal set, so U stays an isometry."""
+def test_truncated_fp32_svd_never_keeps_deflated_zeros():
+    """A truncation keeps only values strictly above its threshold less 2 eps (the
+    oracle's truncate, like the reference's): deflated zeros are dropped even when
+    min_size asks for more values, and the kept factors stay isometries."""
     rng = np.random.default_rng(82)
     t, blocks = _low_rank_tensor(rng, [(30, 24)], [2])
     q.set_gemm_mode("tf32x3")
@@ -194,6 +196,10 @@ def test_truncated_fp32_svd_completes_null_columns_up_to_min_size():
         U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=6, max_size=10 ** 6)
     finally:
         q.set_gemm_mode("f64")
-    assert sum(d.section_sizes) == 6
+    zeros = o.btensor([[(2, 0)], [(2, 0)]], [0], (0,))
+    zeros.blocks = [((0, 0), np.diag([1.0, 0.0]))]
+    Uo, do, Vo = o.svd_truncated(zeros, 1, 1e-14, 6, 10 ** 6)
+    assert [len(v) for _, v in do.blocks] == [1]  # the oracle drops the zero value too
+    assert sum(d.section_sizes) == 2
     assert _isometry_error(U) < 1e-5
     assert _isometry_error(V) < 1e-5
