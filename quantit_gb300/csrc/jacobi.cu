@@ -165,6 +165,7 @@ struct JacobiParams {
     int *sweeps;   // per sector (written at the end)
     int *rotated;  // nsec * max_sweeps flags, zero on entry: a rotation happened in (sector, sweep)
     const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
+    T *dnorm;      // per column (s_off + column): squared norm when deflated, 0 otherwise
 };
 
 // Rotation of one column pair by one warp.  With R > 0 (p <= 32 R) every lane
@@ -176,7 +177,7 @@ struct JacobiParams {
 // Returns whether a column was rotated or deflated.
 template <class T, int R>
 __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ wb, T *__restrict__ va,
-                                            T *__restrict__ vb, int p, int q, int lane, T thr) {
+                                            T *__restrict__ vb, int p, int q, int lane, T thr, T *da, T *db) {
     T al = 0, be = 0, ga = 0;
     T x[R > 0 ? R : 1], y[R > 0 ? R : 1];
     if (R > 0) {
@@ -208,6 +209,10 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
         for (int r = lane; r < p; r += 32) {
             if (za) wa[r] = T(0);
             if (zb) wb[r] = T(0);
+        }
+        if (lane == 0) {
+            if (za) *da = al;
+            if (zb) *db = be;
         }
         return true;
     }
@@ -318,7 +323,10 @@ __global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
             T *wb = P.work + sd.w_off + int64_t(b) * sd.p;
             T *va = P.rot + sd.rot_off + int64_t(a) * sd.q;
             T *vb = P.rot + sd.rot_off + int64_t(b) * sd.q;
-            if (!rotate_pair<T, R>(wa, wb, va, vb, sd.p, sd.q, lane, P.defl ? P.defl[s] : T(0))) continue;
+            T *dn = P.dnorm ? P.dnorm + sd.s_off : nullptr;
+            if (!rotate_pair<T, R>(wa, wb, va, vb, sd.p, sd.q, lane, P.defl ? P.defl[s] : T(0), dn ? dn + a : nullptr,
+                                   dn ? dn + b : nullptr))
+                continue;
             if (lane == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
         }
         grid.sync();
@@ -376,6 +384,7 @@ struct BJacobiParams {
     int upj;       // V work units (row chunks of one CTA width) per job
     int max_q;     // widest sector (columns)
     const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
+    T *dnorm;      // per column (s_off + column): squared norm when deflated, 0 otherwise
 };
 
 __device__ __forceinline__ int bj_items(int q, int B) {
@@ -465,9 +474,10 @@ __device__ __forceinline__ void bj_params_fast(float al, float be, float ga, flo
 // test and rotation as rotate_pair (tol = Eps<T>::tol(p), hoisted by the caller).
 // A zero column (norm 0) is skipped without forming the product; with thr > 0 a
 // column whose squared norm falls to thr or below after the rotation is deflated
-// (set to zero, norm 0).
+// (set to zero, norm 0; dx / dy receive its squared norm before, else stay 0).
 template <class T, int R>
-__device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T thr, T &sn, T &tau) {
+__device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T thr, T &sn, T &tau, T &dx,
+                                          T &dy) {
     if (al == T(0) || be == T(0)) return false;
     const T ga = bj_dot(x, y);
     if (ga == T(0)) return false;
@@ -488,11 +498,13 @@ __device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T 
         if (al <= thr) {
 #pragma unroll
             for (int i = 0; i < R; ++i) x[i] = T(0);
+            dx = al;
             al = T(0);
         }
         if (be <= thr) {
 #pragma unroll
             for (int i = 0; i < R; ++i) y[i] = T(0);
+            dy = be;
             be = T(0);
         }
     }
@@ -683,6 +695,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     // a numerically zero column: deflated (zero from here on)
 #pragma unroll
                     for (int i = 0; i < R; ++i) cols[j * PP + lane + 32 * i] = T(0);
+                    if (lane == 0) P.dnorm[sd.s_off + column(j)] = acc;
                     acc = T(0);
                     zeroed = true;
                 }
@@ -704,8 +717,10 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     if (valid(u) && valid(v)) {
                         bj_load(x, cols + u * PP, lane);
                         bj_load(y, cols + v * PP, lane);
-                        T al = nrm[u], be = nrm[v];
-                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau)) {
+                        T al = nrm[u], be = nrm[v], dx = T(0), dy = T(0);
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy)) {
+                            if (lane == 0 && dx > T(0)) P.dnorm[sd.s_off + column(u)] = dx;
+                            if (lane == 0 && dy > T(0)) P.dnorm[sd.s_off + column(v)] = dy;
                             bj_store(x, cols + u * PP, lane);
                             bj_store(y, cols + v * PP, lane);
                             if (lane < NP) {
@@ -738,8 +753,10 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     const int j = B + (warp + round) % B;
                     if (mine && valid(j)) {
                         bj_load(y, cols + j * PP, lane);
-                        T be = nrm[j];
-                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau)) {
+                        T be = nrm[j], dx = T(0), dy = T(0);
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy)) {
+                            if (lane == 0 && dx > T(0)) P.dnorm[sd.s_off + column(warp)] = dx;
+                            if (lane == 0 && dy > T(0)) P.dnorm[sd.s_off + column(j)] = dy;
                             bj_store(y, cols + j * PP, lane);
                             if (lane < NP) {
                                 T qy = Qs[j * NP + lane];
@@ -848,12 +865,14 @@ template <class T>
 __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, const T *__restrict__ rot,
                                                  double *__restrict__ U, double *__restrict__ V,
                                                  double *__restrict__ S, const SectorDesc *__restrict__ secs,
-                                                 double *__restrict__ scratch, int cap) {
+                                                 double *__restrict__ scratch, int cap, const T *__restrict__ dnorm,
+                                                 int *__restrict__ dpos) {
     extern __shared__ double sh[];
     const SectorDesc sd = secs[blockIdx.x];
     const int q = sd.q, p = sd.p;
     double *sig = sh;                             // q values
     int *perm = reinterpret_cast<int *>(sh + q);  // q ints
+    int *defl = perm + q;                         // q flags: column deflated by the sweeps
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const T *W = work + sd.w_off;
     const T *R = rot + sd.rot_off;
@@ -864,7 +883,13 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
             acc = fma(x, x, acc);
         }
         acc = wsum(acc);
-        if (lane == 0) sig[j] = sqrt(acc);
+        // a deflated column keeps the norm it had when it left the sweeps (a value
+        // below FP32 resolution); its left vector is completed by k_complete_deflated
+        const double dn = (dnorm && acc == 0.0) ? double(dnorm[sd.s_off + j]) : 0.0;
+        if (lane == 0) {
+            sig[j] = dn > 0.0 ? sqrt(dn) : sqrt(acc);
+            defl[j] = dn > 0.0 ? 1 : 0;
+        }
     }
     __syncthreads();
     for (int j = threadIdx.x; j < q; j += blockDim.x) {
@@ -887,14 +912,18 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
         }
         return;
     }
-    for (int j = threadIdx.x; j < q; j += blockDim.x) S[sd.s_off + j] = sig[perm[j]];
+    for (int j = threadIdx.x; j < q; j += blockDim.x) {
+        S[sd.s_off + j] = sig[perm[j]];
+        // 0: resolved column, 1: deflated (left vector to complete), 2: null column
+        if (dpos) dpos[sd.s_off + j] = defl[perm[j]] ? 1 : (sig[perm[j]] > 0.0 ? 0 : 2);
+    }
     // the side built from W (length p): U when !trans, V when trans; the other is R (length q)
     double *Wside = sd.trans ? (V + sd.v_off) : (U + sd.u_off);
     double *Rside = sd.trans ? (U + sd.u_off) : (V + sd.v_off);
     for (int64_t e = threadIdx.x; e < int64_t(q) * p; e += blockDim.x) {
         int j = int(e / p), r = int(e % p);
         double sj = sig[perm[j]];
-        Wside[e] = sj > 0.0 ? double(W[int64_t(perm[j]) * p + r]) / sj : 0.0;
+        Wside[e] = (sj > 0.0 && !defl[perm[j]]) ? double(W[int64_t(perm[j]) * p + r]) / sj : 0.0;
     }
     for (int64_t e = threadIdx.x; e < int64_t(q) * q; e += blockDim.x) {
         int j = int(e / q), r = int(e % q);
@@ -954,6 +983,108 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
             }
             __syncthreads();
         }
+    }
+}
+
+// Left vectors of the deflated columns of the SVD sectors (dpos 1, m of them, in
+// value order).  The resolved columns G (dpos 0, r of them, unit norm) are factored
+// by Householder QR in FP32, G = H_0 ... H_(r-1) R, and the j-th deflated column
+// becomes Q e_(r+j) = H_0 ... H_(r-1) e_(r+j): the completion vectors are orthonormal
+// and orthogonal to G to FP32 accuracy (r + m <= q <= p).  One CTA per sector;
+// scratch at coff[s] holds the p x r reflectors and one p-vector per warp.
+__global__ void __launch_bounds__(1024) k_complete_deflated(double *__restrict__ U, double *__restrict__ V,
+                                                            const SectorDesc *__restrict__ secs,
+                                                            const int *__restrict__ dpos, float *__restrict__ scratch,
+                                                            const int64_t *__restrict__ coff) {
+    extern __shared__ int csh[];  // good positions (q), deflated positions (q), tau (q floats)
+    __shared__ int s_r, s_m;
+    __shared__ float red[32];
+    __shared__ float s_scale;
+    const SectorDesc sd = secs[blockIdx.x];
+    if (sd.mode != 0) return;
+    const int p = sd.p, q = sd.q;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    int *gpos = csh;
+    int *dl = csh + q;
+    float *tau = reinterpret_cast<float *>(csh + 2 * q);
+    if (tid == 0) {
+        int r = 0, m = 0;
+        for (int j = 0; j < q; ++j) {
+            const int f = dpos[sd.s_off + j];
+            if (f == 0) gpos[r++] = j;
+            if (f == 1) dl[m++] = j;
+        }
+        s_r = r;
+        s_m = m;
+    }
+    __syncthreads();
+    const int r = s_r, m = s_m;
+    if (m == 0) return;
+    double *Wside = sd.trans ? (V + sd.v_off) : (U + sd.u_off);
+    float *A = scratch + coff[blockIdx.x];  // p x r, column-major
+    float *xs = A + int64_t(p) * r;         // nw vectors of length p
+    for (int64_t e = tid; e < int64_t(p) * r; e += blockDim.x) {
+        const int c = int(e / p), i = int(e - int64_t(c) * p);
+        A[e] = float(Wside[int64_t(gpos[c]) * p + i]);
+    }
+    __syncthreads();
+    for (int i = 0; i < r; ++i) {
+        float *a = A + int64_t(i) * p;
+        float part = 0.f;
+        for (int k = i + 1 + tid; k < p; k += blockDim.x) part = fmaf(a[k], a[k], part);
+        part = wsum(part);
+        if (lane == 0) red[warp] = part;
+        __syncthreads();
+        if (tid == 0) {
+            float xn2 = 0.f;
+            for (int k = 0; k < nw; ++k) xn2 += red[k];
+            const float alpha = a[i];
+            float t = 0.f, scale = 0.f;
+            if (xn2 > 0.f) {
+                const float beta = -copysignf(sqrtf(fmaf(alpha, alpha, xn2)), alpha);
+                t = (beta - alpha) / beta;
+                scale = 1.f / (alpha - beta);
+            }
+            tau[i] = t;
+            s_scale = scale;
+        }
+        __syncthreads();
+        const float scale = s_scale, ti = tau[i];
+        for (int k = i + 1 + tid; k < p; k += blockDim.x) a[k] *= scale;  // reflector (1, a[i+1:])
+        __syncthreads();
+        if (ti != 0.f) {
+            for (int c = i + 1 + warp; c < r; c += nw) {
+                float *b = A + int64_t(c) * p;
+                float d = 0.f;
+                for (int k = i + 1 + lane; k < p; k += 32) d = fmaf(a[k], b[k], d);
+                d = (wsum(d) + b[i]) * ti;
+                __syncwarp();
+                if (lane == 0) b[i] -= d;
+                for (int k = i + 1 + lane; k < p; k += 32) b[k] = fmaf(-d, a[k], b[k]);
+            }
+        }
+        __syncthreads();
+    }
+    float *x = xs + int64_t(warp) * p;
+    for (int j = warp; j < m; j += nw) {
+        const int col = r + j;
+        for (int k = lane; k < p; k += 32) x[k] = (k == col) ? 1.f : 0.f;
+        __syncwarp();
+        for (int i = r - 1; i >= 0; --i) {
+            const float ti = tau[i];
+            if (ti == 0.f) continue;
+            const float *a = A + int64_t(i) * p;
+            float d = 0.f;
+            for (int k = i + 1 + lane; k < p; k += 32) d = fmaf(a[k], x[k], d);
+            d = (wsum(d) + x[i]) * ti;
+            __syncwarp();
+            if (lane == 0) x[i] -= d;
+            for (int k = i + 1 + lane; k < p; k += 32) x[k] = fmaf(-d, a[k], x[k]);
+            __syncwarp();
+        }
+        double *dst = Wside + int64_t(dl[j]) * p;
+        for (int k = lane; k < p; k += 32) dst[k] = double(x[k]);
+        __syncwarp();
     }
 }
 
@@ -1149,7 +1280,7 @@ void tune_save(const TuneKey &k, int w) {
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
                  int max_sweeps, int *sweeps_out, int *flags, int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes,
-                 const T *defl, cudaStream_t stream) {
+                 const T *defl, T *dnorm, cudaStream_t stream) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
@@ -1164,6 +1295,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
         B.sweeps = sweeps_out;
         B.rotated = flags;
         B.defl = defl;
+        B.dnorm = dnorm;
         B.max_q = max_steps_per_sweep + 1;  // the widest sector's even column count bounds q
         const bool f32 = sizeof(T) == 4;
         const std::vector<int> cands = block_widths(f32, r_class(max_p));
@@ -1221,6 +1353,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     P.sweeps = sweeps_out;
     P.rotated = flags;
     P.defl = defl;
+    P.dnorm = dnorm;
     const int64_t pairs = (sum_q + nsec) / 2 + nsec;  // pairs per step, an upper bound
     // registers per lane: the longest column over the sectors decides
     if (max_p <= 4 * 32)
@@ -1237,15 +1370,15 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
 
 template <class T>
 void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
-                 int max_q, double *scratch, int cap, cudaStream_t stream) {
-    size_t smem = size_t(max_q) * (sizeof(double) + sizeof(int)) + 16;
+                 int max_q, double *scratch, int cap, const T *dnorm, int *dpos, cudaStream_t stream) {
+    size_t smem = size_t(max_q) * (sizeof(double) + 2 * sizeof(int)) + 16;
     static std::once_flag attr;
     std::call_once(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_finish<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
                    "finish smem attribute");
     });
     if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the SVD finishing kernel");
-    k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch, cap);
+    k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch, cap, dnorm, dpos);
     count_launch();
     cuda_check(cudaGetLastError(), "SVD finishing kernel launch");
 }
@@ -1274,23 +1407,39 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl) {
+                      int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm) {
     if (nsec <= 0) return;
+    if ((defl == nullptr) != (dnorm == nullptr)) fail(ERR_INVALID_ARGUMENT, "deflation needs thresholds and norms");
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
                     max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
-                    static_cast<const float *>(defl), stream);
+                    static_cast<const float *>(defl), static_cast<float *>(dnorm), stream);
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
                     max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
-                    static_cast<const double *>(defl), stream);
+                    static_cast<const double *>(defl), static_cast<double *>(dnorm), stream);
 }
 
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
-                   int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl) {
+                   int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm) {
     launch_jacobi_on(ctx().stream, work, rot, sec, slot_start, nsec, max_steps_per_sweep, max_sweeps, sweeps_out, flags,
-                     f32, max_p, sum_q, vwork, vwork_bytes, defl);
+                     f32, max_p, sum_q, vwork, vwork_bytes, defl, dnorm);
+}
+
+void launch_complete_deflated(double *U, double *V, const SectorDesc *sec, int nsec, const int *dpos, float *scratch,
+                              const int64_t *coff, int max_q) {
+    if (nsec <= 0) return;
+    const size_t smem = size_t(max_q) * 3 * sizeof(int);
+    if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the completion kernel");
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cuda_check(cudaFuncSetAttribute(k_complete_deflated, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                   "completion smem attribute");
+    });
+    k_complete_deflated<<<nsec, 1024, smem, ctx().stream>>>(U, V, sec, dpos, scratch, coff);
+    count_launch();
+    cuda_check(cudaGetLastError(), "completion kernel launch");
 }
 
 void launch_deflation_thresholds(const void *work, const SectorDesc *sec, int nsec, double delta, void *thr, int f32) {
@@ -1317,19 +1466,20 @@ size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int 
 }
 
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
-                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap) {
+                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap,
+                      const void *dnorm, int *dpos) {
     if (nsec <= 0) return;
     if (f32)
         finish_impl(static_cast<const float *>(work), static_cast<const float *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch, complete_cap, stream);
+                    scratch, complete_cap, static_cast<const float *>(dnorm), dpos, stream);
     else
         finish_impl(static_cast<const double *>(work), static_cast<const double *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch, complete_cap, stream);
+                    scratch, complete_cap, static_cast<const double *>(dnorm), dpos, stream);
 }
 
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
-                   int max_q, double *scratch, int f32, int complete_cap) {
-    launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32, complete_cap);
+                   int max_q, double *scratch, int f32, int complete_cap, const void *dnorm, int *dpos) {
+    launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32, complete_cap, dnorm, dpos);
 }
 
 }  // namespace qtt

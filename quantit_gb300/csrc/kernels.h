@@ -179,9 +179,17 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 // sweeps (a numerically zero column); null: no deflation.
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
-                   int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0, const void *defl = nullptr);
+                   int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0, const void *defl = nullptr,
+                   void *dnorm = nullptr);
 // thr[s] <- delta^2 ||W_s||_F^2 for every svd sector (0 for eigh), in the work type.
 void launch_deflation_thresholds(const void *work, const SectorDesc *sec, int nsec, double delta, void *thr, int f32);
+// dnorm (with defl; the work type, sum of q entries at s_off, zero on entry) receives
+// the squared norm of every deflated column; launch_finish keeps it as the column's
+// singular value and marks the column in dpos (s_off + output position: 0 resolved,
+// 1 deflated, 2 null), and launch_complete_deflated writes the deflated columns' left
+// vectors.  scratch: FP32, at coff[s] per sector p * (q + 32) elements.
+void launch_complete_deflated(double *U, double *V, const SectorDesc *sec, int nsec, const int *dpos, float *scratch,
+                              const int64_t *coff, int max_q);
 size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int max_sweeps, int f32);
 // Column norms, sort (descending for svd, ascending eigenvalues for eigh),
 // normalisation and completion of null columns; writes U (m x k), V (n x k)
@@ -190,14 +198,16 @@ size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int 
 // completes only the first complete_cap null columns of each sector (in value
 // order): the caller truncates the others away.
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec,
-                   int nsec, int max_q, double *scratch, int f32, int complete_cap = -1);
+                   int nsec, int max_q, double *scratch, int f32, int complete_cap = -1, const void *dnorm = nullptr,
+                   int *dpos = nullptr);
 // The same two launches on an explicit stream (no library context involved).
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
                       int max_p, int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0,
-                      const void *defl = nullptr);
+                      const void *defl = nullptr, void *dnorm = nullptr);
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
-                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap = -1);
+                      const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap = -1,
+                      const void *dnorm = nullptr, int *dpos = nullptr);
 // Segment = one output block (rows x k row-major at dst_off) from a column-major
 // (ld x *) sector matrix at src_off: dst[i*k + j] = src[src_off + (r0 + i) + j*ld].
 struct ScatterEntry {

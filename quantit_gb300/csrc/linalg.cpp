@@ -150,9 +150,11 @@ LastSweeps &last_sweeps() {
 // Set by svd_truncated around the decomposition it runs: its caller keeps only the
 // values the truncation selects, and the truncation never keeps a zero value
 // (btensor_linalg.cpp:658-755 keeps values strictly above the smallest kept one
-// less 2 eps, which is >= 0).  So null columns need no completion, and an FP32
-// sector SVD deflates numerically zero columns (norm <= FP32 epsilon x the sector's
-// Frobenius norm, below what FP32 arithmetic resolves) to exact zeros.
+// less 2 eps, which is >= 0).  So null columns need no completion.  An FP32 sector
+// SVD there also deflates columns whose norm falls to FP32 epsilon x the sector's
+// Frobenius norm (below what FP32 arithmetic resolves): they leave the sweeps, keep
+// that last norm as their singular value, and get an orthonormal completion of the
+// resolved left vectors as theirs, so the factors stay isometries.
 struct TruncHint {
     bool active = false;
     int64_t min_size = 0;
@@ -285,18 +287,37 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
         StatScope sc(ST_SVD, 0.0);
         const size_t vb = jacobi_vwork_bytes(nsec, stot, max_steps, max_sweeps, f32);
         BufPtr vwork = dev_alloc(vb);
-        BufPtr thr;
+        BufPtr thr, dnorm, dpos;
         // a truncation keeps only values above its (non-negative) threshold, never a
         // zero one: null columns need no completion under a truncating svd
         const int cap = (mode == 0 && trunc_hint().active) ? 0 : -1;
-        if (mode == 0 && f32 && trunc_hint().active && svd_deflation()) {
+        const bool deflate = mode == 0 && f32 && trunc_hint().active && svd_deflation();
+        if (deflate) {
             thr = dev_alloc(size_t(nsec) * es);
+            dnorm = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * es);
+            dpos = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * sizeof(int));
+            cuda_check(cudaMemsetAsync(dnorm->p, 0, size_t(std::max<int64_t>(stot, 1)) * es, ctx().stream),
+                       "cudaMemsetAsync(dnorm)");
             launch_deflation_thresholds(W, dsec, nsec, kDeflateF32, thr->p, f32);
         }
         launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
-                      vwork->p, vb, thr ? thr->p : nullptr);
+                      vwork->p, vb, deflate ? thr->p : nullptr, deflate ? dnorm->p : nullptr);
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
-                      static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32, cap);
+                      static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32, cap,
+                      deflate ? dnorm->p : nullptr, deflate ? static_cast<int *>(dpos->p) : nullptr);
+        if (deflate) {
+            // left vectors of the deflated columns: an orthonormal completion (FP32 Householder)
+            std::vector<int64_t> coff(nsec);
+            int64_t ctot = 0;
+            for (int i = 0; i < nsec; ++i) {
+                coff[i] = ctot;
+                ctot += int64_t(D.desc[i].p) * (D.desc[i].q + 32);
+            }
+            BufPtr cs = dev_alloc(size_t(std::max<int64_t>(ctot, 1)) * sizeof(float));
+            launch_complete_deflated(static_cast<double *>(D.U->p), static_cast<double *>(D.V->p), dsec, nsec,
+                                     static_cast<const int *>(dpos->p), static_cast<float *>(cs->p), upload_vec(coff),
+                                     max_q);
+        }
     }
 }
 

@@ -185,21 +185,43 @@ def test_truncated_fp32_svd_deflates_unresolved_columns(kernel):
         np.testing.assert_allclose(R[k], a, atol=1e-5 * float(np.max(np.abs(a))), rtol=0)
 
 
-def test_truncated_fp32_svd_never_keeps_deflated_zeros():
-    """A truncation keeps only values strictly above its threshold less 2 eps (the
-    oracle's truncate, like the reference's): deflated zeros are dropped even when
-    min_size asks for more values, and the kept factors stay isometries."""
+def test_truncated_fp32_svd_completes_deflated_left_vectors():
+    """Deflated columns keep their last norm as singular value (noise below FP32
+    resolution, kept by a small cutoff like the unresolved values of an undeflated
+    FP32 sweep) and get completed left vectors: U stays an isometry."""
     rng = np.random.default_rng(82)
-    t, blocks = _low_rank_tensor(rng, [(30, 24)], [2])
+    t, blocks = _low_rank_tensor(rng, [(30, 24), (50, 41)], [2, 5])
     q.set_gemm_mode("tf32x3")
     try:
         U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=6, max_size=10 ** 6)
     finally:
         q.set_gemm_mode("f64")
-    zeros = o.btensor([[(2, 0)], [(2, 0)]], [0], (0,))
-    zeros.blocks = [((0, 0), np.diag([1.0, 0.0]))]
-    Uo, do, Vo = o.svd_truncated(zeros, 1, 1e-14, 6, 10 ** 6)
-    assert [len(v) for _, v in do.blocks] == [1]  # the oracle drops the zero value too
-    assert sum(d.section_sizes) == 2
+    assert sum(d.section_sizes) >= 7
     assert _isometry_error(U) < 1e-5
     assert _isometry_error(V) < 1e-5
+    R = dict(U.mul(d).tensordot(V.conj(), ([1], [1])).blocks())
+    for k, a in blocks:
+        np.testing.assert_allclose(R[k], a, atol=1e-5 * float(np.max(np.abs(a))), rtol=0)
+
+
+def test_truncated_svd_drops_exact_zero_values_like_the_oracle():
+    """A truncation keeps only values strictly above its threshold less 2 eps, so an
+    exact zero singular value is never kept, whatever min_size asks (the oracle's
+    truncate, btensor_linalg.cpp:658-755); null columns are not completed then."""
+    rng = np.random.default_rng(83)
+    a = np.zeros((30, 24))
+    a[:, :10] = rng.standard_normal((30, 10))
+    legs = [[(30, Z(0))], [(24, Z(0))]]
+    t = q.btensor(legs, Z(0))
+    t.set_blocks([((0, 0), a)])
+    ot = o.btensor([[(30, 0)], [(24, 0)]], [0], (0,))
+    ot.blocks = [((0, 0), a.copy())]
+    Uo, do, Vo = o.svd_truncated(ot, 1, 1e-14, 20, 10 ** 6)
+    for mode in ("f64", "tf32x3"):
+        q.set_gemm_mode(mode)
+        try:
+            U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=20, max_size=10 ** 6)
+        finally:
+            q.set_gemm_mode("f64")
+        assert sum(d.section_sizes) == sum(len(v) for _, v in do.blocks) == 10, mode
+        assert _isometry_error(U) < (1e-11 if mode == "f64" else 1e-5)
