@@ -216,11 +216,11 @@ def test_truncated_svd_drops_exact_zero_values_like_the_oracle():
     t.set_blocks([((0, 0), a)])
     ot = o.btensor([[(30, 0)], [(24, 0)]], [0], (0,))
     ot.blocks = [((0, 0), a.copy())]
-    Uo, do, Vo = o.svd_truncated(ot, 1, 1e-14, 20, 10 ** 6)
+    Uo, do, Vo = o.svd_truncated(ot, 1, 1e-10, 20, 10 ** 6)
     for mode in ("f64", "tf32x3"):
         q.set_gemm_mode(mode)
         try:
-            U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=20, max_size=10 ** 6)
+            U, d, V = q.linalg.svd(t, 1, 1e-10, min_size=20, max_size=10 ** 6)
         finally:
             q.set_gemm_mode("f64")
         assert sum(d.section_sizes) == sum(len(v) for _, v in do.blocks) == 10, mode
