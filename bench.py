@@ -165,6 +165,21 @@ def run_sweeps(q, mpo, mps, n, mode, D):
     return Es, ts, cur
 
 
+def bond_max(mps):
+    """Largest bond dimension of a bMPS (the right leg of each site)."""
+    return int(max(_leg_dim(t, 2) for t in mps))
+
+
+def bond_sum(mps):
+    return int(sum(_leg_dim(t, 2) for t in mps))
+
+
+def _leg_dim(t, leg):
+    sbd = t.sections_by_dim
+    start = sum(sbd[:leg])
+    return int(sum(t.section_sizes[start:start + sbd[leg]]))
+
+
 def fp64_energy(q, mpo, mps):
     t0 = time.perf_counter()
     e, n2 = q.algorithms.mps_energy(mpo, mps)
@@ -505,7 +520,9 @@ def main():
         E64, _ = fp64_energy(q, mpo, mps64)
         cmp = {"fp64_s_per_sweep": float(np.mean(t64)), "speedup_vs_fp64": float(np.mean(t64)) / t_step,
                "dE_per_site": abs(E_mixed - E64) / args.L, "E_fp64": E64, "E_mixed": E_mixed,
-               "energies": "FP64 <psi|H|psi>/<psi|psi> of each path's final state after the same sweeps"}
+               "energies": "FP64 <psi|H|psi>/<psi|psi> of each path's final state after the same sweeps",
+               "bond_dims": {"mixed_max": bond_max(mps2), "fp64_max": bond_max(mps64),
+                             "mixed_sum": bond_sum(mps2), "fp64_sum": bond_sum(mps64)}}
     e2e = e2e_sweep(q, mpo, mps1, args)
     P = peaks()
     pc = {}

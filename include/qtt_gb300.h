@@ -76,10 +76,10 @@ int qtt_get_gemm_mode(void);
 int qtt_set_autotune(int on);
 int qtt_autotune_report(char *buf, int64_t cap, int64_t *len);
 /* Deflation in the FP32 sector SVD of a truncating svd (split GEMM modes only; no
- * reference counterpart): on by default.  A column whose norm falls to FP32 epsilon
- * x its sector's Frobenius norm or below is set to zero and leaves the sweeps; the
- * truncation then discards it (singular values below FP32 resolution).  Off: the
- * sweeps resolve those columns as well. */
+ * reference counterpart): off by default.  On: a column whose norm falls to FP32
+ * epsilon x its sector's Frobenius norm or below leaves the sweeps, keeps that norm
+ * as its singular value, and its left vector is an orthonormal completion of the
+ * resolved ones (FP32 Householder).  Fewer sweeps, plus the cost of the completion. */
 int qtt_set_svd_deflation(int on);
 /* Free and total bytes of the calling thread's device (no reference counterpart;
  * the serving loop admits solves against it). */

@@ -27,7 +27,7 @@ def set_autotune(on):
 
 def set_svd_deflation(on):
     """Deflate columns below FP32 resolution in the mixed path's truncating SVDs
-    (on by default)."""
+    (off by default)."""
     from ._lib import call
     call("qtt_set_svd_deflation", 1 if on else 0)
 

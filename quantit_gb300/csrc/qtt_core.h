@@ -314,7 +314,7 @@ int jacobi_variant();
 // Block-width autotuner of the block-Jacobi kernel (on by default) and its decisions.
 void set_autotune(int on);
 std::string autotune_report();
-// Deflation of numerically zero columns in the FP32 SVD of a truncating svd (on by default).
+// Deflation of numerically zero columns in the FP32 SVD of a truncating svd (off by default).
 void set_svd_deflation(int on);
 int svd_deflation();
 // Non-zero when a tensor-core kernel gave up on a bounded wait since the last

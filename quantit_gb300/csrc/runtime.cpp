@@ -204,7 +204,7 @@ void set_jacobi_variant(int v) {
 }
 int jacobi_variant() { return g_jacobi_variant; }
 namespace {
-std::atomic<int> g_svd_deflation{1};
+std::atomic<int> g_svd_deflation{0};
 }
 void set_svd_deflation(int on) { g_svd_deflation = on ? 1 : 0; }
 int svd_deflation() { return g_svd_deflation; }

@@ -148,12 +148,20 @@ def _isometry_error(F):
     return err
 
 
+@pytest.fixture
+def deflation():
+    q.set_svd_deflation(True)
+    yield
+    q.set_svd_deflation(False)
+
+
 @pytest.mark.parametrize("kernel", ["block", "scalar"])
-def test_truncated_fp32_svd_deflates_unresolved_columns(kernel):
-    """svd with a cutoff on the mixed path: columns whose norm falls below FP32
-    epsilon x their sector's Frobenius norm are deflated to exact zeros and leave
-    the sweeps; the truncation discards them.  The resolved values match LAPACK to
-    FP32 accuracy and the kept factors are isometries."""
+def test_truncated_fp32_svd_deflates_unresolved_columns(kernel, deflation):
+    """svd with a cutoff on the mixed path with deflation on: columns whose norm falls
+    below FP32 epsilon x their sector's Frobenius norm leave the sweeps (never more
+    sweeps than without deflation).  The resolved values match LAPACK to FP32
+    accuracy, the rest stay below FP32 resolution, and the kept factors are
+    isometries."""
     rng = np.random.default_rng(81)
     shapes, ranks = [(150, 130), (90, 80), (40, 40), (12, 9)], [30, 20, 10, 9]
     t, blocks = _low_rank_tensor(rng, shapes, ranks)
@@ -185,7 +193,7 @@ def test_truncated_fp32_svd_deflates_unresolved_columns(kernel):
         np.testing.assert_allclose(R[k], a, atol=1e-5 * float(np.max(np.abs(a))), rtol=0)
 
 
-def test_truncated_fp32_svd_completes_deflated_left_vectors():
+def test_truncated_fp32_svd_completes_deflated_left_vectors(deflation):
     """Deflated columns keep their last norm as singular value (noise below FP32
     resolution, kept by a small cutoff like the unresolved values of an undeflated
     FP32 sweep) and get completed left vectors: U stays an isometry."""
@@ -217,11 +225,13 @@ def test_truncated_svd_drops_exact_zero_values_like_the_oracle():
     ot = o.btensor([[(30, 0)], [(24, 0)]], [0], (0,))
     ot.blocks = [((0, 0), a.copy())]
     Uo, do, Vo = o.svd_truncated(ot, 1, 1e-10, 20, 10 ** 6)
-    for mode in ("f64", "tf32x3"):
+    for mode, defl in (("f64", False), ("tf32x3", False), ("tf32x3", True)):
         q.set_gemm_mode(mode)
+        q.set_svd_deflation(defl)
         try:
             U, d, V = q.linalg.svd(t, 1, 1e-10, min_size=20, max_size=10 ** 6)
         finally:
             q.set_gemm_mode("f64")
+            q.set_svd_deflation(False)
         assert sum(d.section_sizes) == sum(len(v) for _, v in do.blocks) == 10, mode
         assert _isometry_error(U) < (1e-11 if mode == "f64" else 1e-5)
