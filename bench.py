@@ -54,10 +54,14 @@ def parse():
     p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3", "bf16x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving", "contraction"],
+    p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving", "contraction", "svd"],
                    help="dmrg: the D=2048 sweep line (with a short serving section); serving: the full "
                         "Poisson request stream of XXZ solves (L in 16..128, D in 32..512); contraction: the "
-                        "synthetic theta-pair contraction + sector-SVD truncation microbench at D")
+                        "synthetic theta-pair contraction + sector-SVD truncation microbench at D; svd: the "
+                        "truncated sector SVD of a mid-chain DMRG theta at D (after --svd-sweeps sweeps)")
+    p.add_argument("--svd-sweeps", type=int, default=3, help="svd workload: mixed sweeps before the theta is taken")
+    p.add_argument("--save-state", default=None, help="svd workload: write the theta (block-list file)")
+    p.add_argument("--state-file", default=None, help="svd workload: read the theta instead of sweeping")
     p.add_argument("--serving-requests", type=int, default=16)
     p.add_argument("--serving-rate", type=float, default=4.0,
                    help="Poisson arrival rate (requests/s); above the service capacity the stream measures the "
@@ -358,6 +362,62 @@ def serving_section(q, args, full):
     return out
 
 
+def svd_workload(q, args):
+    """The truncated sector SVD svd(theta, 2, 1e-10, 1, D) of the mid-chain two-site
+    theta of a DMRG state (Heisenberg L, D; --svd-sweeps mixed sweeps from the seeded
+    random state), the decomposition a bond update runs.  Each step is one SVD in
+    --mode (the work is the sweeps the decomposition needed), timed with CUDA events
+    on the library stream; L2 is flushed between steps."""
+    import torch
+    from quantit_gb300 import serialize
+    if args.state_file:
+        theta = serialize.load(args.state_file)
+    else:
+        mpo, mps = build_state(q, args.L, args.D, seed=0)
+        _, _, cur = run_sweeps(q, mpo, mps, args.svd_sweeps, "tf32x3", args.D)
+        cur.move_oc(args.L // 2)
+        c = args.L // 2
+        theta = cur[c].tensordot(cur[c + 1], ([2], [0]))
+        if args.save_state:
+            serialize.save(args.save_state, theta)
+    stream = torch.cuda.ExternalStream(q.lib().qtt_get_stream())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    q.set_autotune(False)
+    q.set_gemm_mode(args.mode)
+    try:
+        for _ in range(args.warmup):
+            q.linalg.svd(theta, 2, 1e-10, min_size=1, max_size=args.D)
+        q.stats.reset()
+        q.stats.enable(True)
+        ts = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            U, d, V = q.linalg.svd(theta, 2, 1e-10, min_size=1, max_size=args.D)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        kinds = {k: q.stats.get(k) for k in q.stats.KINDS}
+        q.stats.enable(False)
+        sweeps = q.linalg.last_svd_sweeps()
+    finally:
+        q.set_gemm_mode("f64")
+        q.set_autotune(True)
+    t = float(np.mean(ts))
+    return {"metric": "s per truncated sector SVD of a mid-chain DMRG theta", "value": t, "unit": "s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.mode != "f64" else "f64",
+            "data": "synthetic", "config": {"workload": f"svd(theta, 2, 1e-10, 1, {args.D}) of the mid-chain theta "
+                                                        f"of a Heisenberg L={args.L} D={args.D} DMRG state",
+                                            "sweeps_before": args.svd_sweeps, "mode": args.mode,
+                                            "l2": "flushed between steps (256 MB write)"},
+            "jacobi_sweeps_per_sector": sweeps, "kept": int(sum(d.section_sizes)),
+            "roofline": roofline("svd", kinds["svd"], peaks(), args.mode, {}),
+            "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()}}
+
+
 def contraction_workload(q, args):
     """Synthetic block-sparse contraction + truncation: C[a,s,u,c] = A[a,s,t,b] B[b,t,u,c]
     (bond legs of total D over U(1) charges -8..8, Gaussian section sizes, sigma 3),
@@ -463,8 +523,8 @@ def main():
     import quantit_gb300 as q
     q.ensure_init(local)
     q.set_jacobi_kernel(args.jacobi)
-    if args.workload == "contraction":
-        line = contraction_workload(q, args)
+    if args.workload in ("contraction", "svd"):
+        line = (contraction_workload if args.workload == "contraction" else svd_workload)(q, args)
         if rank == 0:
             print(json.dumps(line))
         if world > 1:

@@ -41,3 +41,13 @@ def eigh(tensor, split=None, upper=False):
     else:
         _lib.call("qtt_eigh_split", tensor._h, int(split), C.byref(d), C.byref(U))
     return btensor._wrap(d), btensor._wrap(U)
+
+
+def last_svd_sweeps():
+    """Jacobi sweeps each sector needed in the calling thread's most recent
+    decomposition (no reference counterpart; synchronises)."""
+    n = C.c_int32()
+    _lib.call("qtt_last_svd_sweeps", None, 0, C.byref(n))
+    buf = (C.c_int32 * max(n.value, 1))()
+    _lib.call("qtt_last_svd_sweeps", buf, n.value, C.byref(n))
+    return list(buf[:n.value])
