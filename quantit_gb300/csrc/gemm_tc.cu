@@ -327,12 +327,7 @@ void launch_gemm_tc(const TcArgs &a, int mode) {
     cuda_check(cudaGetLastError(), "tcgen05 GEMM launch");
 }
 
-int *kernel_error_word() {
-    ctx().tc_used = true;  // the next check reads it
-    return err_word();
-}
-
-// Non-zero when a kernel hit a bounded wait (read and cleared; synchronises).
+// Non-zero when a tensor-core kernel hit a bounded wait (read and cleared; synchronises).
 int tc_error_check() {
     Ctx &c = ctx();
     if (!c.tc_used) return 0;

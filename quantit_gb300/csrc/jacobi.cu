@@ -385,13 +385,7 @@ struct BJacobiParams {
     int max_q;     // widest sector (columns)
     const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
     T *dnorm;      // per column (s_off + column): squared norm when deflated, 0 otherwise
-    int *err;      // device error word: 5 when a bounded hand-off wait gave up
 };
-
-// Bound of a hand-off wait between the warps of one CTA (iterations of one shared-
-// memory load each); the waits form an acyclic chain, so it never expires unless
-// the kernel is broken, and then the error word tells the host.
-constexpr long long HANDOFF_LIMIT = 1ll << 22;
 
 __device__ __forceinline__ int bj_items(int q, int B) {
     if (q < 2) return 0;
@@ -603,7 +597,6 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
     int *sweep = done + nsec;
     int *istart = sweep + nsec;  // nsec + 1 prefix sums of block pairs per step
     __shared__ int ndone, any_rot, s_unit;
-    __shared__ int hand[B];  // inter-block rounds: round after which J column j is free
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool defer_v = P.qbuf != nullptr;
     const int64_t gt = int64_t(blockIdx.x) * NT + tid;
@@ -709,7 +702,6 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                 if (lane == 0) nrm[j] = acc;
             }
             for (int e = tid; e < NP * NP; e += NT) Qs[e] = (e % (NP + 1) == 0) ? T(1) : T(0);
-            if (tid < B) hand[tid] = 0;
             if (tid == 0) any_rot = 0;
             __syncthreads();
             bool rotated_any = zeroed;
@@ -748,10 +740,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                 }
             }
             if (has_b) {
-                // inter-block pairs: warp k keeps I_k, the J columns move through shared
-                // memory.  Column J_jj passes from warp k + 1 (round r - 1) to warp k
-                // (round r): a warp waits only for that hand-off (a release / acquire pair
-                // on hand[jj]), not for a CTA barrier per round.
+                // inter-block pairs: warp k keeps I_k, the J columns move through shared memory
                 const bool mine = valid(warp);
                 T qx = T(0), al = T(0);
                 if (mine) {
@@ -761,20 +750,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                 }
                 bool mine_rot = false;
                 for (int round = 0; round < B; ++round) {
-                    const int jj = (warp + round) % B, j = B + jj;
-                    if (round > 0) {
-                        if (lane == 0) {
-                            long long it = 0;
-                            while (*reinterpret_cast<volatile int *>(&hand[jj]) < round) {
-                                if (++it > HANDOFF_LIMIT) {
-                                    atomicExch(P.err, 5);
-                                    break;
-                                }
-                            }
-                        }
-                        __syncwarp();
-                        __threadfence_block();
-                    }
+                    const int j = B + (warp + round) % B;
                     if (mine && valid(j)) {
                         bj_load(y, cols + j * PP, lane);
                         T be = nrm[j], dx = T(0), dy = T(0);
@@ -791,11 +767,8 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                             mine_rot = true;
                         }
                     }
-                    __threadfence_block();
-                    __syncwarp();
-                    if (lane == 0) *reinterpret_cast<volatile int *>(&hand[jj]) = round + 1;
+                    __syncthreads();
                 }
-                __syncthreads();
                 if (mine_rot) {
                     bj_store(x, cols + warp * PP, lane);
                     if (lane < NP) Qs[warp * NP + lane] = qx;
@@ -1323,7 +1296,6 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
         B.rotated = flags;
         B.defl = defl;
         B.dnorm = dnorm;
-        B.err = kernel_error_word();
         B.max_q = max_steps_per_sweep + 1;  // the widest sector's even column count bounds q
         const bool f32 = sizeof(T) == 4;
         const std::vector<int> cands = block_widths(f32, r_class(max_p));

@@ -104,9 +104,6 @@ struct TcArgs {
 void launch_gemm_tc(const TcArgs &a, int mode);
 // the BF16X3 kernel (called by launch_gemm_tc); err: the context's device error word
 void launch_gemm_bf16x3(const TcArgs &a, int *err, cudaStream_t stream);
-// The calling thread's device error word (kernels that give up a bounded wait write a
-// code: 3 / 4 tensor-core GEMM, 5 block-Jacobi hand-off); marks it for the next check.
-int *kernel_error_word();
 int gemm_tile_m(int mode);
 int gemm_tile_n(int mode);
 

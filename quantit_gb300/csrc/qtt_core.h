@@ -317,12 +317,11 @@ std::string autotune_report();
 // Deflation of numerically zero columns in the FP32 SVD of a truncating svd (off by default).
 void set_svd_deflation(int on);
 int svd_deflation();
-// Non-zero when a kernel gave up on a bounded wait since the last check
-// (synchronises the device; read and cleared).  Codes: 3 / 4 tensor-core GEMM
-// pipeline, 5 block-Jacobi warp hand-off.
+// Non-zero when a tensor-core kernel gave up on a bounded wait since the last
+// check (synchronises the device; read and cleared).
 int tc_error_check();
 inline void tc_error_raise() {
-    if (int e = tc_error_check()) fail(ERR_RUNTIME, "GPU kernel: bounded wait expired (code " + std::to_string(e) + ")");
+    if (int e = tc_error_check()) fail(ERR_RUNTIME, "tensor-core GEMM: bounded wait expired (code " + std::to_string(e) + ")");
 }
 
 // ---------------------------------------------------------------- timing statistics
