@@ -302,19 +302,27 @@ def roofline(kind, st, P, mode, peaks_cache):
 
 
 def e2e_sweep(q, mpo, mps, args):
-    """One sweep through the public API with the MPS uploaded from host buffers and
-    the optimised MPS + energy read back to the host inside the timed region."""
+    """The same sweeps as the device-timed ones (args.steps single sweeps from the same
+    state), each through the public API: the MPS is uploaded from host buffers, one
+    sweep runs, and the optimised MPS and the energy are read back to the host, all
+    inside the timed region; the next sweep starts from those host buffers."""
     host = [(t.copy_structure(), t.blocks()) for t in mps]
-    h2d = sum(sum(v.nbytes for _, v in blks) for _, blks in host)
+    oc = mps.orthogonality_center
     opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=args.D, min_bond=4,
                                      maximum_iterations=1, gemm=args.mode, final_energy_fp64=False)
-    t0 = time.perf_counter()
-    dev = q.networks.bMPS([s.set_blocks(b) for s, b in host], 0)
-    E = q.algorithms.dmrg(mpo, dev, opts)
-    out = [t.blocks() for t in dev]
-    dt = time.perf_counter() - t0
-    d2h = sum(sum(v.nbytes for _, v in blks) for blks in out) + 8
-    return {"value": dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "E": E}
+    ts, h2d, d2h, E = [], [], [], None
+    for _ in range(args.steps):
+        h2d.append(sum(sum(v.nbytes for _, v in blks) for _, blks in host))
+        t0 = time.perf_counter()
+        dev = q.networks.bMPS([s.set_blocks(b) for s, b in host], oc)
+        E = q.algorithms.dmrg(mpo, dev, opts)
+        out = [t.blocks() for t in dev]
+        ts.append(time.perf_counter() - t0)
+        d2h.append(sum(sum(v.nbytes for _, v in blks) for blks in out) + 8)
+        host = [(t.copy_structure(), blks) for t, blks in zip(dev, out)]
+        oc = dev.orthogonality_center
+    return {"value": float(np.mean(ts)), "unit": UNIT, "sweep_times_s": ts,
+            "h2d_bytes_per_step": int(np.mean(h2d)), "d2h_bytes_per_step": int(np.mean(d2h)), "E": E}
 
 
 SERVING_REDUCED = dict(lengths=(16, 32, 64), bonds=(32, 64, 128, 256))
