@@ -187,6 +187,10 @@ typedef struct {
                                       reference counterpart; default 1) */
     int32_t cuda_graphs;           /* k-step Lanczos: capture the two-site matvec once per bond as a CUDA
                                       graph and replay it for the remaining iterations (default 1) */
+    int32_t svd_warm_start;        /* start each bond's sector SVD from the rotation of that bond's
+                                      previous decomposition in this call (no reference counterpart;
+                                      exact for any start; default 1) */
+    int32_t pad;
 } qtt_dmrg_options;
 /* dmrg_options defaults (include/dmrg_options.h:15-58) */
 void qtt_dmrg_options_default(qtt_dmrg_options *opt);

@@ -91,7 +91,7 @@ SIGNATURES = {
 class DmrgOptionsC(C.Structure):
     _fields_ = [("cutoff", f64), ("convergence_criterion", f64), ("maximum_bond", i64), ("minimum_bond", i64),
                 ("maximum_iterations", i64), ("gemm_mode", i32), ("final_energy_fp64", i32),
-                ("lanczos_steps", i32), ("cuda_graphs", i32)]
+                ("lanczos_steps", i32), ("cuda_graphs", i32), ("svd_warm_start", i32), ("pad", i32)]
 
 
 LOG_FN = C.CFUNCTYPE(None, vp, i64, f64, f64)

@@ -13,7 +13,7 @@ class dmrg_options:
 
     def __init__(self, *, cutoff=1e-6, convergence_criterion=1e-5, max_bond=SIZE_MAX, min_bond=4,
                  maximum_iterations=1000, gemm="f64", final_energy_fp64=True, lanczos_steps=1,
-                 cuda_graphs=True):
+                 cuda_graphs=True, svd_warm_start=True):
         self.cutoff = cutoff
         self.convergence_criterion = convergence_criterion
         self.maximum_bond = max_bond
@@ -27,6 +27,8 @@ class dmrg_options:
         self.lanczos_steps = lanczos_steps
         # k-step Lanczos: replay each bond's matvec from a captured CUDA graph
         self.cuda_graphs = cuda_graphs
+        # start each bond's sector SVD from that bond's previous rotation (exact either way)
+        self.svd_warm_start = svd_warm_start
 
     def _c(self):
         o = _lib.DmrgOptionsC()
@@ -39,6 +41,7 @@ class dmrg_options:
         o.final_energy_fp64 = int(bool(self.final_energy_fp64))
         o.lanczos_steps = int(self.lanczos_steps)
         o.cuda_graphs = int(bool(self.cuda_graphs))
+        o.svd_warm_start = int(bool(self.svd_warm_start))
         return o
 
 

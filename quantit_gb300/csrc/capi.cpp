@@ -382,6 +382,8 @@ void qtt_dmrg_options_default(qtt_dmrg_options *o) {
     o->final_energy_fp64 = 1;
     o->lanczos_steps = 1;
     o->cuda_graphs = 1;
+    o->svd_warm_start = 1;
+    o->pad = 0;
 }
 int qtt_compute_2sites_hamil(qtt_bt wl, qtt_bt wr, qtt_bt *out) {
     return guarded([&] {
@@ -449,6 +451,7 @@ int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_d
             o.final_energy_fp64 = opt->final_energy_fp64;
             o.lanczos_steps = opt->lanczos_steps > 0 ? opt->lanczos_steps : 1;
             o.cuda_graphs = opt->cuda_graphs;
+            o.svd_warm_start = opt->svd_warm_start;
         }
         *E0 = qtt::dmrg(W, S, *oc, o, log_fn, log_user);
         for (int i = 0; i < L; ++i) mps[i] = wrap(std::move(S[i]));

@@ -382,6 +382,8 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
     // generate_env (dmrg.cpp:371-409); env[i+1] holds Env[i]
     int64_t oc = oc_io;
     std::vector<BT> env(L + 2);
+    // per bond: the sector rotations of its last decomposition in this call (warm starts)
+    std::vector<WarmStart> warm(opt.svd_warm_start ? size_t(std::max<int64_t>(L, 1)) : 0);
     env[0] = trivial_edge(mps[0], 0, mpo[0], 0);
     env[L + 1] = trivial_edge(mps[L - 1], 2, mpo[L - 1], 2);
     for (int64_t i = 0; i < oc; ++i) env[i + 1] = compute_left_env(mpo[i], mps[i], env[i]);
@@ -426,7 +428,8 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
                 cuda_check(cudaMemcpyAsync(hscal, scal, 7 * sizeof(double), cudaMemcpyDeviceToHost, ctx().stream),
                            "cudaMemcpyAsync(scalars)");
             }
-            SVDOut f = svd_truncated(upd, 2, opt.cutoff, opt.minimum_bond, opt.maximum_bond, 2.0);  // syncs
+            SVDOut f = svd_truncated(upd, 2, opt.cutoff, opt.minimum_bond, opt.maximum_bond, 2.0,
+                                     warm.empty() ? nullptr : &warm[size_t(oc)]);  // syncs
             if (hscal[6] != 0.0) fail(ERR_LOGIC, "nan found in output tensor");
             E = hscal[3];
             // d /= sqrt(sum(d.pow(2)))  (dmrg.cpp:188)

@@ -17,6 +17,7 @@ struct DmrgOpts {
     int final_energy_fp64 = 1;  // mixed modes: return the FP64 <psi|H|psi>/<psi|psi> of the final state
     int lanczos_steps = 1;      // 1: QuantiT's one-step update; k > 1: k-step Lanczos (lanczos_k)
     int cuda_graphs = 1;        // k-step Lanczos: replay the matvec from a captured CUDA graph
+    int svd_warm_start = 1;     // start each bond's sector SVD from its previous rotation (this call)
 };
 // k-step Lanczos with full reorthogonalisation: the lowest Ritz value and its
 // (normalised) Ritz vector of the two-site effective Hamiltonian.

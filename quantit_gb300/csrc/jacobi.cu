@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
     for (int s = 0; s < nsec; ++s) {
         const SectorDesc sd = P.secs[s];
         const int64_t qq = int64_t(sd.q) * sd.q;
+        if (sd.warm) continue;  // rot already holds the warm start V0
         for (int64_t e = gt; e < qq; e += nt) P.rot[sd.rot_off + e] = (e % (sd.q + 1) == 0) ? T(1) : T(0);
     }
     if (threadIdx.x == 0) ndone = 0;
@@ -605,6 +606,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
     for (int s = 0; s < nsec; ++s) {
         const SectorDesc sd = P.secs[s];
         const int64_t qq = int64_t(sd.q) * sd.q;
+        if (sd.warm) continue;  // rot already holds the warm start V0
         for (int64_t e = gt; e < qq; e += nt) P.rot[sd.rot_off + e] = (e % (sd.q + 1) == 0) ? T(1) : T(0);
     }
     if (tid == 0) {
@@ -1088,6 +1090,79 @@ __global__ void __launch_bounds__(1024) k_complete_deflated(double *__restrict__
     }
 }
 
+// Warm start: tmp = W V0 per sector in 64 x 64 tiles (256 threads, 4 x 4 outputs each,
+// K slabs of 16 through shared memory), then (mode 1) work <- tmp and rot <- V0.
+template <class T>
+__global__ void __launch_bounds__(256) k_warm_gemm(const T *__restrict__ work, T *__restrict__ tmp,
+                                                   const WarmDesc *__restrict__ wd, int nwarm) {
+    __shared__ T As[16][64 + 1];
+    __shared__ T Bs[16][64 + 1];
+    int lo = 0, hi = nwarm - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (wd[mid].tile_start <= int(blockIdx.x))
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const WarmDesc d = wd[lo];
+    const int p = d.p, q = d.q;
+    const int tm = (p + 63) / 64;
+    const int t = int(blockIdx.x) - d.tile_start;
+    const int r0 = (t % tm) * 64, c0 = (t / tm) * 64;
+    const T *W = work + d.w_off;
+    const T *V0 = static_cast<const T *>(d.v0);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+    for (int k0 = 0; k0 < q; k0 += 16) {
+        for (int e = threadIdx.x; e < 16 * 64; e += 256) {
+            const int kk = e / 64, i = e % 64;  // A: rows contiguous
+            const int r = r0 + i, k = k0 + kk;
+            As[kk][i] = (r < p && k < q) ? W[int64_t(k) * p + r] : T(0);
+            const int jj = e / 16, kb = e % 16;  // B: k contiguous within a column of V0
+            const int c = c0 + jj, kq = k0 + kb;
+            Bs[kb][jj] = (c < q && kq < q) ? V0[int64_t(c) * q + kq] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            T a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
+            if (r < p && c < q) tmp[d.w_off + int64_t(c) * p + r] = acc[i][j];
+        }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_warm_commit(T *__restrict__ work, T *__restrict__ rot,
+                                                     const T *__restrict__ tmp, const WarmDesc *__restrict__ wd) {
+    const WarmDesc d = wd[blockIdx.y];
+    const int64_t nw = int64_t(d.p) * d.q, nr = int64_t(d.q) * d.q;
+    const T *V0 = static_cast<const T *>(d.v0);
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nw; e += int64_t(gridDim.x) * blockDim.x)
+        work[d.w_off + e] = tmp[d.w_off + e];
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nr; e += int64_t(gridDim.x) * blockDim.x)
+        rot[d.rot_off + e] = V0[e];
+}
+
 int sm_count() {
     static std::once_flag once;
     static int nsm = 0;
@@ -1425,6 +1500,26 @@ void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot
                    int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm) {
     launch_jacobi_on(ctx().stream, work, rot, sec, slot_start, nsec, max_steps_per_sweep, max_sweeps, sweeps_out, flags,
                      f32, max_p, sum_q, vwork, vwork_bytes, defl, dnorm);
+}
+
+void launch_warm_apply(void *work, void *rot, void *tmp, const WarmDesc *wd, int nwarm, int ntiles, int f32) {
+    if (nwarm <= 0 || ntiles <= 0) return;
+    if (f32) {
+        k_warm_gemm<float><<<ntiles, 256, 0, ctx().stream>>>(static_cast<const float *>(work),
+                                                               static_cast<float *>(tmp), wd, nwarm);
+        k_warm_commit<float><<<dim3(64, nwarm), 256, 0, ctx().stream>>>(static_cast<float *>(work),
+                                                                        static_cast<float *>(rot),
+                                                                        static_cast<const float *>(tmp), wd);
+    } else {
+        k_warm_gemm<double><<<ntiles, 256, 0, ctx().stream>>>(static_cast<const double *>(work),
+                                                                static_cast<double *>(tmp), wd, nwarm);
+        k_warm_commit<double><<<dim3(64, nwarm), 256, 0, ctx().stream>>>(static_cast<double *>(work),
+                                                                         static_cast<double *>(rot),
+                                                                         static_cast<const double *>(tmp), wd);
+    }
+    count_launch();
+    count_launch();
+    cuda_check(cudaGetLastError(), "warm-start kernel launch");
 }
 
 void launch_complete_deflated(double *U, double *V, const SectorDesc *sec, int nsec, const int *dpos, float *scratch,

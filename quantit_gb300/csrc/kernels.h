@@ -150,8 +150,19 @@ struct SectorDesc {
     int32_t m, n, p, q;
     int32_t trans;  // 1 when W = A^T
     int32_t mode;   // 0: svd, 1: eigh (symmetric input, shifted to positive definite)
+    int32_t warm;   // 1: rot holds an orthogonal start V0 and work holds W V0 (warm start)
+    int32_t pad;
     double shift;   // eigh: diagonal shift added before the sweeps
 };
+// Warm start of one sector SVD: work[w_off ..] (p x q, column-major) <- W V0 with V0 the
+// q x q orthogonal matrix at v0 (the work type), and rot[rot_off ..] <- V0.  tmp: scratch
+// with the work buffer's offsets.  Tiles of 64 x 64 outputs, tile_start = prefix sums.
+struct WarmDesc {
+    int64_t w_off, rot_off;
+    const void *v0;
+    int32_t p, q, tile_start, pad;
+};
+void launch_warm_apply(void *work, void *rot, void *tmp, const WarmDesc *wd, int nwarm, int ntiles, int f32);
 // Segment = one input block (rows x cols at src_off) placed at rows [r0, r0+rows),
 // cols [c0, c0+cols) of sector `sector`.
 struct PackEntry {

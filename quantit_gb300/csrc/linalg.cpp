@@ -158,6 +158,7 @@ LastSweeps &last_sweeps() {
 struct TruncHint {
     bool active = false;
     int64_t min_size = 0;
+    WarmStart *ws = nullptr;  // warm starts of the decomposition (svd only)
 };
 TruncHint &trunc_hint() {
     thread_local TruncHint h;
@@ -165,7 +166,10 @@ TruncHint &trunc_hint() {
 }
 struct ScopedTruncHint {
     TruncHint saved;
-    ScopedTruncHint(bool on, int64_t min_size) : saved(trunc_hint()) { trunc_hint() = TruncHint{on, min_size}; }
+    ScopedTruncHint(bool on, int64_t min_size, WarmStart *ws)
+        : saved(trunc_hint()) {
+        trunc_hint() = TruncHint{on, min_size, ws};
+    }
     ~ScopedTruncHint() { trunc_hint() = saved; }
 };
 constexpr double kDeflateF32 = 1.1920928955078125e-07;  // FP32 epsilon (2^-23)
@@ -252,6 +256,41 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             }
         }
     }
+    // warm starts: a sector whose key (shape, batch element, q-side sections) matches an
+    // entry of the previous decomposition at this bond starts from that rotation
+    WarmStart *ws = mode == 0 ? trunc_hint().ws : nullptr;
+    std::vector<std::vector<int64_t>> keys;
+    std::vector<WarmDesc> wdesc;
+    int ntiles = 0;
+    if (ws) {
+        for (size_t g = 0; g < D.secs.size(); ++g) {
+            const Sector &s = D.secs[g];
+            for (int64_t e = 0; e < s.batch; ++e) {
+                SectorDesc &d = D.desc[D.first_desc[g] + e];
+                std::vector<int64_t> key = {d.trans, d.m, d.n, e};
+                key.insert(key.end(), s.lead.begin(), s.lead.end());
+                for (const SecRow &sr : (d.trans ? s.rows : s.cols)) {
+                    key.push_back(sr.sec);
+                    key.push_back(sr.size);
+                }
+                for (const WarmStart::Entry &en : ws->entries) {
+                    if (en.f32 != f32 || en.key != key || d.q < 2) continue;
+                    d.warm = 1;
+                    WarmDesc w{};
+                    w.w_off = d.w_off;
+                    w.rot_off = d.rot_off;
+                    w.v0 = static_cast<const char *>(en.buf->p) + en.off * int64_t(es);
+                    w.p = d.p;
+                    w.q = d.q;
+                    w.tile_start = ntiles;
+                    ntiles += ((d.p + 63) / 64) * ((d.q + 63) / 64);
+                    wdesc.push_back(w);
+                    break;
+                }
+                keys.push_back(std::move(key));
+            }
+        }
+    }
     SectorDesc *dsec = static_cast<SectorDesc *>(upload(D.desc.data(), D.desc.size() * sizeof(SectorDesc)));
     auto chunks = make_chunks(lens);
     {
@@ -300,6 +339,10 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
                        "cudaMemsetAsync(dnorm)");
             launch_deflation_thresholds(W, dsec, nsec, kDeflateF32, thr->p, f32);
         }
+        if (!wdesc.empty()) {
+            BufPtr tmp = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * es);
+            launch_warm_apply(W, D.rot->p, tmp->p, upload_vec(wdesc), int(wdesc.size()), ntiles, f32);
+        }
         launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
                       vwork->p, vb, deflate ? thr->p : nullptr, deflate ? dnorm->p : nullptr);
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
@@ -317,6 +360,13 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             launch_complete_deflated(static_cast<double *>(D.U->p), static_cast<double *>(D.V->p), dsec, nsec,
                                      static_cast<const int *>(dpos->p), static_cast<float *>(cs->p), upload_vec(coff),
                                      max_q);
+        }
+        if (ws) {
+            // this decomposition's rotations start the next one at the same bond
+            std::vector<WarmStart::Entry> next;
+            for (int i = 0; i < nsec; ++i)
+                next.push_back(WarmStart::Entry{std::move(keys[i]), D.rot, D.desc[i].rot_off, f32});
+            ws->entries = std::move(next);
         }
     }
 }
@@ -626,10 +676,11 @@ SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, dou
     return o;
 }
 
-SVDOut svd_truncated(const BT &t, int64_t split, double tol, int64_t min_size, int64_t max_size, double pw) {
+SVDOut svd_truncated(const BT &t, int64_t split, double tol, int64_t min_size, int64_t max_size, double pw,
+                     WarmStart *ws) {
     SVDOut full;
     {
-        ScopedTruncHint hint(tol > 0.0, min_size);
+        ScopedTruncHint hint(tol > 0.0, min_size, ws);
         full = svd_split(t, split);
     }
     return truncate(std::move(full), max_size, min_size, tol, pw, true);

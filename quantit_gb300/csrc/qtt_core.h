@@ -284,7 +284,23 @@ struct SVDOut {
 SVDOut svd(const BT &t);                       // untruncated, rank >= 2, sectors on the last two legs
 SVDOut svd_split(const BT &t, int64_t split);  // svd(A, split)
 SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, double pw, bool has_v = true);
-SVDOut svd_truncated(const BT &t, int64_t split, double tol, int64_t min_size, int64_t max_size, double pw);
+// Orthogonal start matrices for the sector SVDs at one bond: the q-side rotation V of
+// each sector of the previous decomposition there, keyed by the sector's shape and
+// q-side sections.  Any orthogonal start V0 gives an exact SVD (W = (W V0) V0^T, and
+// the sweeps accumulate into V0); one from an unchanged basis leaves W V0 nearly
+// column-orthogonal, and the Jacobi needs a few sweeps instead of tens.
+struct WarmStart {
+    struct Entry {
+        std::vector<int64_t> key;
+        BufPtr buf;   // the rotation buffer of that decomposition
+        int64_t off;  // element offset of the sector's q x q matrix in buf
+        int f32;      // element type: float (mixed path) or double
+    };
+    std::vector<Entry> entries;
+};
+// ws (optional): warm starts read from and written back to ws.
+SVDOut svd_truncated(const BT &t, int64_t split, double tol, int64_t min_size, int64_t max_size, double pw,
+                     WarmStart *ws = nullptr);
 struct EighOut {
     BT d, U;
 };
