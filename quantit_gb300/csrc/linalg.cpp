@@ -256,8 +256,9 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             }
         }
     }
-    // warm starts: a sector whose key (shape, batch element, q-side sections) matches an
-    // entry of the previous decomposition at this bond starts from that rotation
+    // warm starts: a sector whose key (orientation, batch element, q-side sections) matches
+    // an entry of the previous decomposition at this bond starts from that rotation; the
+    // long side may differ (W V0 is defined for any number of rows)
     WarmStart *ws = mode == 0 ? trunc_hint().ws : nullptr;
     std::vector<std::vector<int64_t>> keys;
     std::vector<WarmDesc> wdesc;
@@ -267,7 +268,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             const Sector &s = D.secs[g];
             for (int64_t e = 0; e < s.batch; ++e) {
                 SectorDesc &d = D.desc[D.first_desc[g] + e];
-                std::vector<int64_t> key = {d.trans, d.m, d.n, e};
+                std::vector<int64_t> key = {d.trans, d.q, e};
                 key.insert(key.end(), s.lead.begin(), s.lead.end());
                 for (const SecRow &sr : (d.trans ? s.rows : s.cols)) {
                     key.push_back(sr.sec);

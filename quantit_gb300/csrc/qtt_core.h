@@ -285,8 +285,8 @@ SVDOut svd(const BT &t);                       // untruncated, rank >= 2, sector
 SVDOut svd_split(const BT &t, int64_t split);  // svd(A, split)
 SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, double pw, bool has_v = true);
 // Orthogonal start matrices for the sector SVDs at one bond: the q-side rotation V of
-// each sector of the previous decomposition there, keyed by the sector's shape and
-// q-side sections.  Any orthogonal start V0 gives an exact SVD (W = (W V0) V0^T, and
+// each sector of the previous decomposition there, keyed by the sector's orientation
+// and q-side sections.  Any orthogonal start V0 gives an exact SVD (W = (W V0) V0^T, and
 // the sweeps accumulate into V0); one from an unchanged basis leaves W V0 nearly
 // column-orthogonal, and the Jacobi needs a few sweeps instead of tens.
 struct WarmStart {
