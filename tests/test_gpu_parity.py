@@ -253,3 +253,27 @@ def test_dmrg_exact_energy_L8():
     E = q.algorithms.dmrg(mpo, mps, q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=1e-13,
                                                               max_bond=16, maximum_iterations=20))
     assert E == pytest.approx(e0, abs=1e-9)
+
+
+@pytest.mark.parametrize("gemm, tol", [("f64", 1e-10), ("tf32x3", 1e-8)])
+def test_dmrg_svd_warm_start_is_exact(gemm, tol):
+    """Each bond's sector SVD may start from the rotation of its previous decomposition
+    in the call: any orthogonal start gives an exact SVD, so the energies agree with
+    cold starts (FP64: 1e-10 relative, structures equal; mixed: FP32-level)."""
+    L, D = 12, 40
+    mpo = o.heisenberg_mpo(L)
+    mps = o.right_canonicalize(o.random_mps(L, D, [1, -1], 0, np.random.default_rng(8)))
+    dmpo = q.networks.bMPO([to_device(t) for t in mpo])
+    out = {}
+    for warm in (False, True):
+        dmps = q.networks.bMPS([to_device(t) for t in mps], 0)
+        log = q.algorithms.dmrg_log_sweeptime()
+        q.algorithms.dmrg(dmpo, dmps, q.algorithms.dmrg_options(
+            cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4, maximum_iterations=4, gemm=gemm,
+            svd_warm_start=warm), log)
+        e, n2 = q.algorithms.mps_energy(dmpo, dmps)
+        out[warm] = (e / n2, dmps)
+    assert abs(out[True][0] - out[False][0]) <= tol * abs(out[False][0])
+    if gemm == "f64":
+        for a, b in zip(out[True][1], out[False][1]):
+            assert a.block_indices() == b.block_indices()
