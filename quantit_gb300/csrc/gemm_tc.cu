@@ -9,22 +9,27 @@
 //
 // Two kernels:
 //  * k_split_tf32: one pass over the operand blocks writes hi / lo as FP32 bit
-//    patterns in matrix form (rows x K4, K contiguous, zero padded to a multiple
-//    of 4).  The FP64 -> FP32 conversion uses integer operations only: GB300's FP64
-//    pipe is a small fraction of its FP32 / integer rate.
+//    patterns in the tensor cores' core-matrix tiling: rows padded to 8 and K to 8,
+//    each 8-row x 4-element core matrix (128 bytes) contiguous, the core matrices of
+//    a row group in K order.  A row group's slice of a K chunk is then one contiguous
+//    block of memory.  The FP64 -> FP32 conversion uses integer operations only:
+//    GB300's FP64 pipe is a small fraction of its FP32 / integer rate.
 //  * k_gemm_tf32x3: CTA = one 128 x 128 tile of one output block (same tile and
-//    pair tables as the FP64 kernel).  All 8 warps copy 16-byte vectors of the
-//    split operands into a 3-stage shared-memory ring in the canonical no-swizzle
-//    K-major UMMA layout (core matrices of 8 rows x 16 bytes).  Thread 0 issues
-//    the tcgen05.mma instructions of a stage (3 products x 4 k-steps of 8) and
-//    commits them to that stage's mbarrier, which the producers wait on before
-//    refilling the stage.  The epilogue reads the accumulator with tcgen05.ld and
-//    writes alpha*acc + beta*add in FP64 (a plain integer widening when alpha = 1
-//    and there is no add term).
+//    pair tables as the FP64 kernel), warp-specialised:
+//      - warp 0 (producer) fills a 3-stage shared-memory ring with bulk asynchronous
+//        copies (cp.async.bulk, one per row group and operand copy), counted in bytes
+//        on the stage's "full" mbarrier; the shared layout is the canonical
+//        no-swizzle K-major UMMA layout (LBO 128 B, SBO 1024 B);
+//      - one thread of warp 1 waits on "full", issues the stage's tcgen05.mma
+//        (3 products x up to 4 k-steps of 8) and commits them to the stage's "empty"
+//        mbarrier, which the producer waits on before refilling the stage;
+//      - after the last stage it commits to "done", and all warps run the epilogue:
+//        tcgen05.ld of the accumulator, alpha*acc + beta*add in FP64 (a plain integer
+//        widening when alpha = 1 and there is no add term).
 //
 // Every mbarrier wait is bounded; on timeout the kernel records an error code in
-// a device word that the host checks, still waits (bounded) for its MMAs and
-// frees its TMEM before returning.
+// a device word that the host checks, drains (bounded) the copies and MMAs it
+// issued and frees its TMEM before returning.
 #include <cstdint>
 #include <mutex>
 
@@ -52,7 +57,9 @@ using tc::mbar_wait;
 using tc::amax_shift;
 using tc::f64_to_f32_int;
 using tc::f32_to_f64_int;
-using tc::st_shared_v4;
+using tc::mbar_expect_tx;
+using tc::bulk_g2s;
+using tc::umma_commit;
 static_assert(SBO == (TBK * 4 / 16) * 128, "the shared layout assumes 128-byte rows per K chunk");
 
 // kind::tf32, D=F32, A=B=TF32, both K-major, N=128, M=128
@@ -99,37 +106,9 @@ __global__ void k_split_tf32(const double *__restrict__ src, float *__restrict__
         const uint32_t h = to_tf32(xf);
         const uint32_t l = to_tf32(xf - __uint_as_float(h));
         const int64_t row = lin / e.K, k = lin - row * e.K;
-        const int64_t dst = e.dst_off + row * e.K4 + k;
+        const int64_t dst = e.dst_off + ((row >> 3) * (e.K4 >> 2) + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3);
         hi[dst] = __uint_as_float(h);
         lo[dst] = __uint_as_float(l);
-    }
-}
-
-// byte offset of (row r, k) in one operand copy of the canonical K-major layout
-__device__ __forceinline__ uint32_t kmaj_off(int r, int k) {
-    return uint32_t(r >> 3) * SBO + uint32_t(k >> 2) * LBO + uint32_t(r & 7) * 16u + uint32_t(k & 3) * 4u;
-}
-
-// rows x (TBK / 4) 16-byte vectors of one operand tile (hi and lo) into shared memory
-template <int ROWS>
-__device__ __forceinline__ void load_tile(const float *__restrict__ hi, const float *__restrict__ lo, int64_t off,
-                                          int rows_valid, int row0, int K4, int k0, char *shi, char *slo, int tid) {
-#pragma unroll
-    for (int i = 0; i < (ROWS * (TBK / 4)) / TTHREADS; ++i) {
-        const int e = tid + i * TTHREADS;
-        // eight consecutive threads take eight consecutive rows of one core matrix
-        // (one contiguous 128-byte store per quarter warp, no bank conflicts)
-        const int row = ((e >> 6) << 3) | (e & 7), kc = (e >> 3) & 7;
-        const int gr = row0 + row, gk = k0 + kc * 4;
-        uint4 vh = make_uint4(0, 0, 0, 0), vl = make_uint4(0, 0, 0, 0);
-        if (gr < rows_valid && gk < K4) {
-            const int64_t idx = off + int64_t(gr) * K4 + gk;
-            vh = __ldg(reinterpret_cast<const uint4 *>(hi + idx));
-            vl = __ldg(reinterpret_cast<const uint4 *>(lo + idx));
-        }
-        const uint32_t so = kmaj_off(row, kc * 4);
-        st_shared_v4(shi + so, vh);
-        st_shared_v4(slo + so, vl);
     }
 }
 
@@ -143,9 +122,9 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t da, uint64_t db
 __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err) {
     extern __shared__ __align__(1024) char smem_raw[];
     char *smem = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ uint64_t mbar[NSTAGE];
+    __shared__ uint64_t full[NSTAGE], empty[NSTAGE], done;
     __shared__ uint32_t tmem_base_sh;
-    __shared__ int abort_flag;
+    __shared__ int abort_flag, n_issued, n_consumed;
 
     const GemmTile t = g.tiles[blockIdx.x];
     const GemmOut o = g.outs[t.out];
@@ -157,9 +136,15 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(&mbar[s], 1);
+        for (int s = 0; s < NSTAGE; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;");
         abort_flag = 0;
+        n_issued = 0;
+        n_consumed = 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -167,40 +152,69 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
     const uint32_t tmem = tmem_base_sh;
 
     int nchunk = 0;
-    for (int p = o.p0; p < o.p1; ++p) nchunk += ((g.pairs[p].K + 3) / 4 * 4 + TBK - 1) / TBK;
+    for (int p = o.p0; p < o.p1; ++p) nchunk += (((g.pairs[p].K + 7) & ~7) + TBK - 1) / TBK;
 
-    int p = o.p0, k0 = 0;
-    uint32_t commits[NSTAGE] = {};
-    for (int c = 0; c < nchunk; ++c) {
-        const int s = c % NSTAGE;
-        if (c >= NSTAGE) {
-            if (!mbar_wait(&mbar[s], (commits[s] - 1) & 1)) {
-                if (tid == 0) atomicExch(err, 1);
-                abort_flag = 1;
+    if (warp == 0) {
+        // producer: one bulk copy per (operand copy, row group) of each K chunk
+        const float *srcs[4] = {static_cast<const float *>(g.Ahi), static_cast<const float *>(g.Alo),
+                                static_cast<const float *>(g.Bhi), static_cast<const float *>(g.Blo)};
+        const int rga = min(TBM / 8, (o.M - t.m0 + 7) / 8), rgb = min(TBN / 8, (o.N - t.n0 + 7) / 8);
+        int p = o.p0, k0 = 0, c = 0;
+        for (; c < nchunk; ++c) {
+            const int s = c % NSTAGE;
+            int ok = 1;
+            if (lane == 0 && c >= NSTAGE) ok = mbar_wait(&empty[s], ((c / NSTAGE) - 1) & 1) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                if (lane == 0) {
+                    atomicExch(err, 1);
+                    atomicExch(&abort_flag, 1);
+                }
+                break;
             }
+            while (k0 >= ((g.pairs[p].K + 7) & ~7)) {
+                ++p;
+                k0 = 0;
+            }
+            const GemmPair pr = g.pairs[p];
+            const int KP = (pr.K + 7) & ~7, kv = min(TBK, KP - k0);
+            const uint32_t rg_bytes = uint32_t(kv) * 32u;  // kv / 4 core matrices of 128 bytes
+            if (lane == 0) mbar_expect_tx(&full[s], 2u * rg_bytes * uint32_t(rga + rgb));
+            __syncwarp();
+            char *st = smem + s * STAGE_BYTES;
+            const int nA = 2 * rga, ncopy = 2 * (rga + rgb);
+            for (int i = lane; i < ncopy; i += 32) {
+                const bool isA = i < nA;
+                const int j = isA ? i : i - nA, which = j & 1, rg = j >> 1;
+                const int64_t grg = (isA ? t.m0 : t.n0) / 8 + rg;
+                const float *src = srcs[(isA ? 0 : 2) + which] + (isA ? pr.a_off : pr.b_off) +
+                                   (grg * (KP / 4) + k0 / 4) * 32;
+                char *dst = st + (isA ? 0 : 2 * A_BYTES) + which * (isA ? A_BYTES : B_BYTES) + rg * int(SBO);
+                bulk_g2s(dst, src, rg_bytes, &full[s]);
+            }
+            k0 += TBK;
         }
-        __syncthreads();
-        if (abort_flag) break;
-        while (k0 >= ((g.pairs[p].K + 3) & ~3)) {
-            ++p;
-            k0 = 0;
-        }
-        const GemmPair pr = g.pairs[p];
-        const int K4 = (pr.K + 3) & ~3;
-        char *st = smem + s * STAGE_BYTES;
-        char *ahi = st, *alo = st + A_BYTES, *bhi = st + 2 * A_BYTES, *blo = st + 2 * A_BYTES + B_BYTES;
-        load_tile<TBM>(static_cast<const float *>(g.Ahi), static_cast<const float *>(g.Alo), pr.a_off, o.M, t.m0, K4, k0, ahi, alo, tid);
-        load_tile<TBN>(static_cast<const float *>(g.Bhi), static_cast<const float *>(g.Blo), pr.b_off, o.N, t.n0, K4, k0, bhi, blo, tid);
-        k0 += TBK;
-        // make the generic-proxy stores visible to the tensor core
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
+        if (lane == 0) n_issued = c;
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        const uint32_t idesc = idesc_tf32();
+        int p = o.p0, k0 = 0, c = 0;
+        for (; c < nchunk; ++c) {
+            const int s = c % NSTAGE;
+            if (!mbar_wait(&full[s], (c / NSTAGE) & 1)) {
+                atomicExch(err, 2);
+                atomicExch(&abort_flag, 1);
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t idesc = idesc_tf32();
-            const uint32_t a_hi = smem_u32(ahi), a_lo = smem_u32(alo), b_hi = smem_u32(bhi), b_lo = smem_u32(blo);
-#pragma unroll
-            for (int ks = 0; ks < TBK / 8; ++ks) {
+            while (k0 >= ((g.pairs[p].K + 7) & ~7)) {
+                ++p;
+                k0 = 0;
+            }
+            const int kv = min(TBK, ((g.pairs[p].K + 7) & ~7) - k0);
+            char *st = smem + s * STAGE_BYTES;
+            const uint32_t a_hi = smem_u32(st), a_lo = a_hi + A_BYTES, b_hi = a_hi + 2 * A_BYTES, b_lo = b_hi + B_BYTES;
+            for (int ks = 0; ks < kv / 8; ++ks) {
                 const uint32_t koff = uint32_t(ks) * 2u * LBO;  // 8 tf32 = 2 core matrices along K
                 const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
                 // small terms first, then the leading product
@@ -208,17 +222,20 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
                 mma_tf32(tmem, make_desc(a_lo + koff), make_desc(b_hi + koff), idesc, 1u);
                 mma_tf32(tmem, make_desc(a_hi + koff), make_desc(b_hi + koff), idesc, 1u);
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&mbar[s]))
-                         : "memory");
+            umma_commit(&empty[s]);
+            k0 += TBK;
         }
-        commits[s] += 1;
+        n_consumed = c;
+        umma_commit(&done);
     }
-    for (int s = 0; s < NSTAGE; ++s) {
-        if (commits[s] == 0) continue;
-        if (!mbar_wait(&mbar[s], (commits[s] - 1) & 1)) {
-            if (tid == 0) atomicExch(err, 2);
-        }
+    // everyone: the accumulator is final once "done" fires
+    if (lane == 0 && !mbar_wait(&done, 0)) atomicExch(err, 2);
+    __syncwarp();
+    __syncthreads();
+    if (tid == 0) {
+        // copies issued but never consumed (only after a timeout) must land before exit
+        for (int c = n_consumed; c < n_issued; ++c)
+            if (!mbar_wait(&full[c % NSTAGE], (c / NSTAGE) & 1)) atomicExch(err, 2);
     }
     asm volatile("tcgen05.fence::after_thread_sync;");
     __syncthreads();

@@ -69,8 +69,9 @@ void launch_gemm_f64(const GemmArgs &a);
 // Segment = one operand block; element e of the (rows x K) matrix reads
 // src[src_off + sum_d idx_d(e) * stride[d]] with idx(e) the row-major index over dims.
 struct SplitEntry {
-    int64_t src_off, dst_off;  // dst_off: element offset into the split arrays, a multiple of the K granule
-    // K4: the padded row length (K rounded up to 4 for TF32X3, to 8 for BF16X3)
+    int64_t src_off, dst_off;  // dst_off: element offset of the block in the split arrays
+    // K4: the padded K (K rounded up to 8); TF32X3 blocks are tiled in 8 x 4 core
+    // matrices (rows padded to 8), BF16X3 blocks are row-major rows of K4
     int32_t rank, K, K4, pad;
     int64_t dims[8];
     int64_t stride[8];
@@ -87,9 +88,9 @@ void launch_amax(const double *x, int64_t n, unsigned long long *amax);
 // rows padded to K8 = (K + 7) & ~7 elements; the same amax scaling.
 void launch_split_bf16x3(const double *src, void *hi, void *mid, void *lo, const SplitEntry *e, const Chunk *chunks,
                          int64_t nchunks, const unsigned long long *amax);
-// A pair's a_off / b_off index the split arrays; A rows = M, B rows = N.  Rows are padded
-// to K4 = (K + 3) & ~3 floats (TF32X3: hi / lo, mid unused) or K8 = (K + 7) & ~7 bf16
-// (BF16X3: hi / mid / lo).
+// A pair's a_off / b_off index the split arrays; A rows = M, B rows = N, K padded to
+// K8 = (K + 7) & ~7 (TF32X3: hi / lo in core-matrix tiling, mid unused; BF16X3:
+// hi / mid / lo row-major).
 struct TcArgs {
     const void *Ahi, *Amid, *Alo, *Bhi, *Bmid, *Blo;
     const unsigned long long *amax_a, *amax_b;  // operand scales (see launch_split_tf32)

@@ -45,6 +45,29 @@ static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
     return false;
 }
 
+// Arrive on an mbarrier and add `bytes` to its expected transaction count.
+static __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Asynchronous bulk copy global -> this CTA's shared memory (16-byte aligned addresses,
+// size a multiple of 16); completion is counted in bytes on `bar`.
+static __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Commit the calling thread's prior tcgen05.mma operations to an mbarrier (one arrival
+// when they have completed).
+static __device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
 // Exponent of an operand's max |x| (the scale 2^-shift brings it to [1, 2));
 // zero, infinite or NaN maxima leave the operand unscaled.
 static __device__ __forceinline__ int amax_shift(unsigned long long bits) {
