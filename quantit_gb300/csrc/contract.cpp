@@ -266,13 +266,13 @@ int64_t prod_sizes(const BT &t, int64_t b, const std::vector<int64_t> &dims) {
 
 namespace {
 // Split every block of t (legs permuted by perm; the first nrow legs form the
-// rows, the rest the contracted K) into hi / lo TF32 arrays (TF32X3: core-matrix
-// tiling, rows and K zero padded to 8) or hi / mid / lo BF16 arrays (BF16X3: rows of
-// K zero padded to 8).
+// rows, the rest the contracted K) into hi / lo TF32 arrays (TF32X3) or hi / mid / lo
+// BF16 arrays (BF16X3), tiled in the tensor cores' core matrices (8 rows x 16 bytes),
+// rows zero padded to 8 and K to the MMA's K step (8 TF32 / 16 BF16).
 void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std::vector<int64_t> &offs, BufPtr &hi,
                    BufPtr &mid, BufPtr &lo, unsigned long long *amax, int mode) {
     const bool bf16 = mode == GEMM_BF16X3;
-    const int64_t gran = 8;
+    const int64_t gran = bf16 ? 16 : 8;
     const int r = t.rank;
     const int64_t nb = t.nblocks();
     offs.assign(nb, 0);
@@ -304,7 +304,7 @@ void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std:
         e.K4 = int32_t(K4);
         offs[b] = o;
         lens[b] = rows * K;
-        o += (bf16 ? rows : (rows + 7) & ~int64_t(7)) * K4;
+        o += ((rows + 7) & ~int64_t(7)) * K4;
     }
     const size_t bytes = size_t(std::max<int64_t>(o, 8)) * (bf16 ? sizeof(uint16_t) : sizeof(float));
     std::vector<BufPtr *> parts = {&hi, &lo};

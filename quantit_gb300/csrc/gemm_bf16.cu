@@ -10,13 +10,13 @@
 // BF16 products cost the tensor time of three TF32 products (BF16 runs at twice the
 // TF32 rate) and move 3 x 2 bytes per operand element instead of 2 x 4.
 //
-// Layout and pipeline follow k_gemm_tf32x3: one 128 x 128 output tile per CTA,
-// 8 warps copy 16-byte vectors of the split operands (rows x K8, K contiguous,
-// zero padded to a multiple of 8) into the canonical no-swizzle K-major layout
-// (128-byte rows per K chunk of 64 bf16), a 2-stage ring of 96 KB stages, thread 0
-// issues 6 products x 4 k-steps of 16 per stage and commits them to the stage's
-// mbarrier.  Every wait is bounded; on timeout the kernel records an error code,
-// still waits (bounded) for its MMAs and frees its TMEM.
+// Layout and pipeline follow k_gemm_tf32x3: the split operands are tiled in core
+// matrices of 8 rows x 8 bf16 (128 bytes; rows padded to 8, K to 16), one 128 x 128
+// output tile per CTA, a producer warp fills a 4-stage ring (48 KB stages: K chunks
+// of 32 bf16, hi / mid / lo of A and B) with one bulk asynchronous copy per operand
+// copy and row group, one thread issues 6 products x 2 k-steps of 16 per stage and
+// commits them to the stage's "empty" mbarrier.  Every wait is bounded; on timeout
+// the kernel records an error code, drains what it issued and frees its TMEM.
 #include <cstdint>
 #include <mutex>
 
@@ -27,16 +27,25 @@
 namespace qtt {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;  // tile and K chunk (bf16 elements: 128 bytes per row)
+constexpr int BM = 128, BN = 128, BK = 32;  // tile and K chunk (bf16 elements: 64 bytes per row)
 constexpr int BTHREADS = 256;
 constexpr int BTMEM_COLS = 128;
-constexpr int COPY_BYTES = 128 * BK * 2;           // one operand copy (hi, mid or lo): 16 KB
-constexpr int BSTAGE_BYTES = 6 * COPY_BYTES;       // hi/mid/lo of A and B: 96 KB
-constexpr int BNSTAGE = 2;
+constexpr uint32_t BSBO = (BK * 2 / 16) * 128;     // next 8-row group: 4 core matrices along K (512 B)
+constexpr int COPY_BYTES = 128 * BK * 2;           // one operand copy (hi, mid or lo): 8 KB
+constexpr int BSTAGE_BYTES = 6 * COPY_BYTES;       // hi/mid/lo of A and B: 48 KB
+constexpr int BNSTAGE = 4;
 constexpr int BSMEM_BYTES = BNSTAGE * BSTAGE_BYTES + 1024;
 using tc::LBO;
-using tc::SBO;
-static_assert(SBO == (BK * 2 / 16) * 128, "the shared layout assumes 128-byte rows per K chunk");
+
+// no-swizzle K-major descriptor with this kernel's 8-row-group stride
+__device__ __forceinline__ uint64_t make_desc_b(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= uint64_t((saddr & 0x3FFFF) >> 4);
+    d |= uint64_t(LBO >> 4) << 16;
+    d |= uint64_t(BSBO >> 4) << 32;
+    d |= uint64_t(1) << 46;
+    return d;
+}
 
 // kind::f16, D=F32, A=B=BF16, both K-major, N=128, M=128
 __host__ __device__ constexpr uint32_t idesc_bf16() {
@@ -72,40 +81,10 @@ __global__ void k_split_bf16x3(const double *__restrict__ src, uint16_t *__restr
         const uint16_t m = to_bf16(r1);
         const uint16_t l = to_bf16(r1 - from_bf16(m));
         const int64_t row = lin / e.K, k = lin - row * e.K;
-        const int64_t dst = e.dst_off + row * e.K4 + k;
+        const int64_t dst = e.dst_off + ((row >> 3) * (e.K4 >> 3) + (k >> 3)) * 64 + (row & 7) * 8 + (k & 7);
         hi[dst] = h;
         mid[dst] = m;
         lo[dst] = l;
-    }
-}
-
-// byte offset of (row r, bf16 element k) in one operand copy of the canonical K-major layout
-__device__ __forceinline__ uint32_t kmaj_off16(int r, int k) {
-    return uint32_t(r >> 3) * SBO + uint32_t(k >> 3) * LBO + uint32_t(r & 7) * 16u + uint32_t(k & 7) * 2u;
-}
-
-// ROWS x 8 16-byte vectors (8 bf16 each) of the three copies of one operand tile
-template <int ROWS>
-__device__ __forceinline__ void load_tile3(const uint16_t *__restrict__ s0, const uint16_t *__restrict__ s1,
-                                           const uint16_t *__restrict__ s2, int64_t off, int rows_valid, int row0,
-                                           int K8, int k0, char *d0, char *d1, char *d2, int tid) {
-#pragma unroll
-    for (int i = 0; i < (ROWS * 8) / BTHREADS; ++i) {
-        const int e = tid + i * BTHREADS;
-        // eight consecutive threads take eight consecutive rows of one core matrix
-        const int row = ((e >> 6) << 3) | (e & 7), kc = (e >> 3) & 7;
-        const int gr = row0 + row, gk = k0 + kc * 8;
-        uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0, v2 = v0;
-        if (gr < rows_valid && gk < K8) {
-            const int64_t idx = off + int64_t(gr) * K8 + gk;
-            v0 = __ldg(reinterpret_cast<const uint4 *>(s0 + idx));
-            v1 = __ldg(reinterpret_cast<const uint4 *>(s1 + idx));
-            v2 = __ldg(reinterpret_cast<const uint4 *>(s2 + idx));
-        }
-        const uint32_t so = kmaj_off16(row, kc * 8);
-        tc::st_shared_v4(d0 + so, v0);
-        tc::st_shared_v4(d1 + so, v1);
-        tc::st_shared_v4(d2 + so, v2);
     }
 }
 
@@ -119,17 +98,13 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db
 __global__ void __launch_bounds__(BTHREADS, 1) k_gemm_bf16x3(TcArgs g, int *err) {
     extern __shared__ __align__(1024) char smem_raw[];
     char *smem = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ uint64_t mbar[BNSTAGE];
+    __shared__ uint64_t full[BNSTAGE], empty[BNSTAGE], done;
     __shared__ uint32_t tmem_base_sh;
-    __shared__ int abort_flag;
+    __shared__ int abort_flag, n_issued, n_consumed;
 
     const GemmTile t = g.tiles[blockIdx.x];
     const GemmOut o = g.outs[t.out];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint16_t *Ah = static_cast<const uint16_t *>(g.Ahi), *Am = static_cast<const uint16_t *>(g.Amid),
-                   *Al = static_cast<const uint16_t *>(g.Alo);
-    const uint16_t *Bh = static_cast<const uint16_t *>(g.Bhi), *Bm = static_cast<const uint16_t *>(g.Bmid),
-                   *Bl = static_cast<const uint16_t *>(g.Blo);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -138,9 +113,15 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_gemm_bf16x3(TcArgs g, int *err)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int s = 0; s < BNSTAGE; ++s) tc::mbar_init(&mbar[s], 1);
+        for (int s = 0; s < BNSTAGE; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(&done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;");
         abort_flag = 0;
+        n_issued = 0;
+        n_consumed = 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -148,62 +129,93 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_gemm_bf16x3(TcArgs g, int *err)
     const uint32_t tmem = tmem_base_sh;
 
     int nchunk = 0;
-    for (int p = o.p0; p < o.p1; ++p) nchunk += (((g.pairs[p].K + 7) & ~7) + BK - 1) / BK;
+    for (int p = o.p0; p < o.p1; ++p) nchunk += (((g.pairs[p].K + 15) & ~15) + BK - 1) / BK;
 
-    int p = o.p0, k0 = 0;
-    uint32_t commits[BNSTAGE] = {};
-    for (int c = 0; c < nchunk; ++c) {
-        const int s = c % BNSTAGE;
-        if (c >= BNSTAGE) {
-            if (!tc::mbar_wait(&mbar[s], (commits[s] - 1) & 1)) {
-                if (tid == 0) atomicExch(err, 3);
-                abort_flag = 1;
+    if (warp == 0) {
+        // producer: one bulk copy per (operand copy, row group) of each K chunk
+        const uint16_t *srcs[6] = {static_cast<const uint16_t *>(g.Ahi), static_cast<const uint16_t *>(g.Amid),
+                                   static_cast<const uint16_t *>(g.Alo), static_cast<const uint16_t *>(g.Bhi),
+                                   static_cast<const uint16_t *>(g.Bmid), static_cast<const uint16_t *>(g.Blo)};
+        const int rga = min(BM / 8, (o.M - t.m0 + 7) / 8), rgb = min(BN / 8, (o.N - t.n0 + 7) / 8);
+        int p = o.p0, k0 = 0, c = 0;
+        for (; c < nchunk; ++c) {
+            const int s = c % BNSTAGE;
+            int ok = 1;
+            if (lane == 0 && c >= BNSTAGE) ok = tc::mbar_wait(&empty[s], ((c / BNSTAGE) - 1) & 1) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                if (lane == 0) {
+                    atomicExch(err, 3);
+                    atomicExch(&abort_flag, 1);
+                }
+                break;
             }
+            while (k0 >= ((g.pairs[p].K + 15) & ~15)) {
+                ++p;
+                k0 = 0;
+            }
+            const GemmPair pr = g.pairs[p];
+            const int KP = (pr.K + 15) & ~15, kv = min(BK, KP - k0);
+            const uint32_t rg_bytes = uint32_t(kv) * 16u;  // kv / 8 core matrices of 128 bytes
+            if (lane == 0) tc::mbar_expect_tx(&full[s], 3u * rg_bytes * uint32_t(rga + rgb));
+            __syncwarp();
+            char *st = smem + s * BSTAGE_BYTES;
+            const int nA = 3 * rga, ncopy = 3 * (rga + rgb);
+            for (int i = lane; i < ncopy; i += 32) {
+                const bool isA = i < nA;
+                const int j = isA ? i : i - nA, which = j % 3, rg = j / 3;
+                const int64_t grg = (isA ? t.m0 : t.n0) / 8 + rg;
+                const uint16_t *src = srcs[(isA ? 0 : 3) + which] + (isA ? pr.a_off : pr.b_off) +
+                                      (grg * (KP / 8) + k0 / 8) * 64;
+                char *dst = st + ((isA ? 0 : 3) + which) * COPY_BYTES + rg * int(BSBO);
+                tc::bulk_g2s(dst, src, rg_bytes, &full[s]);
+            }
+            k0 += BK;
         }
-        __syncthreads();
-        if (abort_flag) break;
-        while (k0 >= ((g.pairs[p].K + 7) & ~7)) {
-            ++p;
-            k0 = 0;
-        }
-        const GemmPair pr = g.pairs[p];
-        const int K8 = (pr.K + 7) & ~7;
-        char *st = smem + s * BSTAGE_BYTES;
-        char *ah = st, *am = st + COPY_BYTES, *al = st + 2 * COPY_BYTES;
-        char *bh = st + 3 * COPY_BYTES, *bm = st + 4 * COPY_BYTES, *bl = st + 5 * COPY_BYTES;
-        load_tile3<BM>(Ah, Am, Al, pr.a_off, o.M, t.m0, K8, k0, ah, am, al, tid);
-        load_tile3<BN>(Bh, Bm, Bl, pr.b_off, o.N, t.n0, K8, k0, bh, bm, bl, tid);
-        k0 += BK;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
+        if (lane == 0) n_issued = c;
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        const uint32_t idesc = idesc_bf16();
+        int p = o.p0, k0 = 0, c = 0;
+        for (; c < nchunk; ++c) {
+            const int s = c % BNSTAGE;
+            if (!tc::mbar_wait(&full[s], (c / BNSTAGE) & 1)) {
+                atomicExch(err, 4);
+                atomicExch(&abort_flag, 1);
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t idesc = idesc_bf16();
-            const uint32_t a0 = tc::smem_u32(ah), a1 = tc::smem_u32(am), a2 = tc::smem_u32(al);
-            const uint32_t b0 = tc::smem_u32(bh), b1 = tc::smem_u32(bm), b2 = tc::smem_u32(bl);
-#pragma unroll
-            for (int ks = 0; ks < BK / 16; ++ks) {
+            while (k0 >= ((g.pairs[p].K + 15) & ~15)) {
+                ++p;
+                k0 = 0;
+            }
+            const int kv = min(BK, ((g.pairs[p].K + 15) & ~15) - k0);
+            const uint32_t base = tc::smem_u32(smem + s * BSTAGE_BYTES);
+            const uint32_t a0 = base, a1 = base + COPY_BYTES, a2 = base + 2 * COPY_BYTES;
+            const uint32_t b0 = base + 3 * COPY_BYTES, b1 = base + 4 * COPY_BYTES, b2 = base + 5 * COPY_BYTES;
+            for (int ks = 0; ks < kv / 16; ++ks) {
                 const uint32_t koff = uint32_t(ks) * 2u * LBO;  // 16 bf16 = 2 core matrices along K
                 const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
                 // second-order terms first, then first order, then the leading product
-                mma_bf16(tmem, tc::make_desc(a0 + koff), tc::make_desc(b2 + koff), idesc, acc0);
-                mma_bf16(tmem, tc::make_desc(a1 + koff), tc::make_desc(b1 + koff), idesc, 1u);
-                mma_bf16(tmem, tc::make_desc(a2 + koff), tc::make_desc(b0 + koff), idesc, 1u);
-                mma_bf16(tmem, tc::make_desc(a0 + koff), tc::make_desc(b1 + koff), idesc, 1u);
-                mma_bf16(tmem, tc::make_desc(a1 + koff), tc::make_desc(b0 + koff), idesc, 1u);
-                mma_bf16(tmem, tc::make_desc(a0 + koff), tc::make_desc(b0 + koff), idesc, 1u);
+                mma_bf16(tmem, make_desc_b(a0 + koff), make_desc_b(b2 + koff), idesc, acc0);
+                mma_bf16(tmem, make_desc_b(a1 + koff), make_desc_b(b1 + koff), idesc, 1u);
+                mma_bf16(tmem, make_desc_b(a2 + koff), make_desc_b(b0 + koff), idesc, 1u);
+                mma_bf16(tmem, make_desc_b(a0 + koff), make_desc_b(b1 + koff), idesc, 1u);
+                mma_bf16(tmem, make_desc_b(a1 + koff), make_desc_b(b0 + koff), idesc, 1u);
+                mma_bf16(tmem, make_desc_b(a0 + koff), make_desc_b(b0 + koff), idesc, 1u);
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             tc::smem_u32(&mbar[s]))
-                         : "memory");
+            tc::umma_commit(&empty[s]);
+            k0 += BK;
         }
-        commits[s] += 1;
+        n_consumed = c;
+        tc::umma_commit(&done);
     }
-    for (int s = 0; s < BNSTAGE; ++s) {
-        if (commits[s] == 0) continue;
-        if (!tc::mbar_wait(&mbar[s], (commits[s] - 1) & 1)) {
-            if (tid == 0) atomicExch(err, 4);
-        }
+    if (lane == 0 && !tc::mbar_wait(&done, 0)) atomicExch(err, 4);
+    __syncwarp();
+    __syncthreads();
+    if (tid == 0) {
+        for (int c = n_consumed; c < n_issued; ++c)
+            if (!tc::mbar_wait(&full[c % BNSTAGE], (c / BNSTAGE) & 1)) atomicExch(err, 4);
     }
     asm volatile("tcgen05.fence::after_thread_sync;");
     __syncthreads();

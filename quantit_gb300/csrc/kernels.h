@@ -70,8 +70,9 @@ void launch_gemm_f64(const GemmArgs &a);
 // src[src_off + sum_d idx_d(e) * stride[d]] with idx(e) the row-major index over dims.
 struct SplitEntry {
     int64_t src_off, dst_off;  // dst_off: element offset of the block in the split arrays
-    // K4: the padded K (K rounded up to 8); TF32X3 blocks are tiled in 8 x 4 core
-    // matrices (rows padded to 8), BF16X3 blocks are row-major rows of K4
+    // K4: the padded K (rounded up to 8 for TF32X3, 16 for BF16X3); blocks are tiled in
+    // core matrices of 8 rows x 16 bytes (rows padded to 8), a row group's core
+    // matrices in K order
     int32_t rank, K, K4, pad;
     int64_t dims[8];
     int64_t stride[8];
@@ -84,13 +85,12 @@ void launch_split_tf32(const double *src, float *hi, float *lo, const SplitEntry
 // *amax (zeroed by the caller) <- max(*amax, bits of |x|) over n doubles (bit order =
 // value order for non-negative doubles, so the maximum is exact and deterministic).
 void launch_amax(const double *x, int64_t n, unsigned long long *amax);
-// Split-BF16 variant: hi / mid / lo bf16 (uint16) arrays in the same matrix form with
-// rows padded to K8 = (K + 7) & ~7 elements; the same amax scaling.
+// Split-BF16 variant: hi / mid / lo bf16 (uint16) arrays in the same tiling (core
+// matrices of 8 rows x 8 elements, K padded to 16); the same amax scaling.
 void launch_split_bf16x3(const double *src, void *hi, void *mid, void *lo, const SplitEntry *e, const Chunk *chunks,
                          int64_t nchunks, const unsigned long long *amax);
-// A pair's a_off / b_off index the split arrays; A rows = M, B rows = N, K padded to
-// K8 = (K + 7) & ~7 (TF32X3: hi / lo in core-matrix tiling, mid unused; BF16X3:
-// hi / mid / lo row-major).
+// A pair's a_off / b_off index the split arrays (core-matrix tiling); A rows = M,
+// B rows = N (TF32X3: hi / lo, mid unused; BF16X3: hi / mid / lo).
 struct TcArgs {
     const void *Ahi, *Amid, *Alo, *Bhi, *Bmid, *Blo;
     const unsigned long long *amax_a, *amax_b;  // operand scales (see launch_split_tf32)
