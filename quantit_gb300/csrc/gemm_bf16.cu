@@ -12,9 +12,9 @@
 //
 // Layout and pipeline follow k_gemm_tf32x3: the split operands are tiled in core
 // matrices of 8 rows x 8 bf16 (128 bytes; rows padded to 8, K to 16), one 128 x 128
-// output tile per CTA, a producer warp fills a 4-stage ring (48 KB stages: K chunks
-// of 32 bf16, hi / mid / lo of A and B) with one bulk asynchronous copy per operand
-// copy and row group, one thread issues 6 products x 2 k-steps of 16 per stage and
+// output tile per CTA, a producer warp fills a 2-stage ring (96 KB stages: K chunks
+// of 64 bf16, hi / mid / lo of A and B) with one bulk asynchronous copy (1 KB) per
+// operand copy and row group, one thread issues 6 products x 4 k-steps of 16 per stage and
 // commits them to the stage's "empty" mbarrier.  Every wait is bounded; on timeout
 // the kernel records an error code, drains what it issued and frees its TMEM.
 #include <cstdint>
@@ -27,13 +27,13 @@
 namespace qtt {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 32;  // tile and K chunk (bf16 elements: 64 bytes per row)
+constexpr int BM = 128, BN = 128, BK = 64;  // tile and K chunk (bf16 elements: 128 bytes per row)
 constexpr int BTHREADS = 256;
 constexpr int BTMEM_COLS = 128;
-constexpr uint32_t BSBO = (BK * 2 / 16) * 128;     // next 8-row group: 4 core matrices along K (512 B)
-constexpr int COPY_BYTES = 128 * BK * 2;           // one operand copy (hi, mid or lo): 8 KB
-constexpr int BSTAGE_BYTES = 6 * COPY_BYTES;       // hi/mid/lo of A and B: 48 KB
-constexpr int BNSTAGE = 4;
+constexpr uint32_t BSBO = (BK * 2 / 16) * 128;     // next 8-row group: 8 core matrices along K (1 KB)
+constexpr int COPY_BYTES = 128 * BK * 2;           // one operand copy (hi, mid or lo): 16 KB
+constexpr int BSTAGE_BYTES = 6 * COPY_BYTES;       // hi/mid/lo of A and B: 96 KB
+constexpr int BNSTAGE = 2;
 constexpr int BSMEM_BYTES = BNSTAGE * BSTAGE_BYTES + 1024;
 using tc::LBO;
 
