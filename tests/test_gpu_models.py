@@ -67,12 +67,13 @@ def test_hubbard_mixed_matches_fp64():
     base = dict(cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=1)
     q.algorithms.dmrg(mpo, mps, q.algorithms.dmrg_options(maximum_iterations=40, gemm="f64", **base))
     out = {}
-    for gemm in ("f64", "tf32x3"):
+    for gemm in ("f64", "tf32x3", "bf16x3"):
         cur = NET.bMPS(list(mps), mps.orthogonality_center)
         q.algorithms.dmrg(mpo, cur, q.algorithms.dmrg_options(maximum_iterations=3, gemm=gemm, **base))
         e, n2 = q.algorithms.mps_energy(mpo, cur)
         out[gemm] = e / n2
-    assert abs(out["tf32x3"] - out["f64"]) / L < 1e-8, out
+    for gemm in ("tf32x3", "bf16x3"):
+        assert abs(out[gemm] - out["f64"]) / L < 1e-8, (gemm, out)
 
 
 def test_cylinder_dmrg_matches_oracle():
@@ -105,9 +106,11 @@ def test_cylinder_mixed_matches_fp64():
     base = dict(cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=1)
     q.algorithms.dmrg(mpo, mps, q.algorithms.dmrg_options(maximum_iterations=8, gemm="f64", **base))
     out = {}
-    for gemm in ("f64", "tf32x3"):
+    # config 3: split-TF32 and split-BF16 GEMMs against FP64 from the same state
+    for gemm in ("f64", "tf32x3", "bf16x3"):
         cur = NET.bMPS(list(mps), mps.orthogonality_center)
         q.algorithms.dmrg(mpo, cur, q.algorithms.dmrg_options(maximum_iterations=2, gemm=gemm, **base))
         e, n2 = q.algorithms.mps_energy(mpo, cur)
         out[gemm] = e / n2
-    assert abs(out["tf32x3"] - out["f64"]) / L < 1e-8, out
+    for gemm in ("tf32x3", "bf16x3"):
+        assert abs(out[gemm] - out["f64"]) / L < 1e-8, (gemm, out)
