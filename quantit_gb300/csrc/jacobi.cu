@@ -863,12 +863,14 @@ __global__ void __launch_bounds__(256) k_defl_thr(const T *__restrict__ work, co
 
 // One CTA per sector: column norms, ordering, normalisation, completion.
 // scratch: at least p doubles per sector at offset w_off (the candidate vector).
+// perm_out (with cap == 0): the CTA only orders the columns (S, perm_out at s_off) and
+// k_finish_copy writes the factors with many CTAs per sector.
 template <class T>
 __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, const T *__restrict__ rot,
                                                  double *__restrict__ U, double *__restrict__ V,
                                                  double *__restrict__ S, const SectorDesc *__restrict__ secs,
                                                  double *__restrict__ scratch, int cap, const T *__restrict__ dnorm,
-                                                 int *__restrict__ dpos) {
+                                                 int *__restrict__ dpos, int *__restrict__ perm_out) {
     extern __shared__ double sh[];
     const SectorDesc sd = secs[blockIdx.x];
     const int q = sd.q, p = sd.p;
@@ -905,9 +907,12 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
         perm[rk] = j;
     }
     __syncthreads();
+    if (perm_out)
+        for (int j = threadIdx.x; j < q; j += blockDim.x) perm_out[sd.s_off + j] = perm[j];
     if (sd.mode == 1) {
         const int n = q;
         for (int j = threadIdx.x; j < n; j += blockDim.x) S[sd.s_off + j] = sig[perm[j]] - sd.shift;
+        if (perm_out) return;
         for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
             int j = int(e / n), r = int(e % n);
             U[sd.u_off + e] = double(R[int64_t(perm[j]) * n + r]);
@@ -919,6 +924,7 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
         // 0: resolved column, 1: deflated (left vector to complete), 2: null column
         if (dpos) dpos[sd.s_off + j] = defl[perm[j]] ? 1 : (sig[perm[j]] > 0.0 ? 0 : 2);
     }
+    if (perm_out) return;  // k_finish_copy writes the factors
     // the side built from W (length p): U when !trans, V when trans; the other is R (length q)
     double *Wside = sd.trans ? (V + sd.v_off) : (U + sd.u_off);
     double *Rside = sd.trans ? (U + sd.u_off) : (V + sd.v_off);
@@ -1161,6 +1167,39 @@ __global__ void __launch_bounds__(256) k_warm_commit(T *__restrict__ work, T *__
         work[d.w_off + e] = tmp[d.w_off + e];
     for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nr; e += int64_t(gridDim.x) * blockDim.x)
         rot[d.rot_off + e] = V0[e];
+}
+
+// The factor writes of k_finish spread over many CTAs per sector (grid: chunks of
+// 2048 elements x sectors): the W side W[:, perm[j]] / s_j (zero for null or deflated
+// columns), the R side R[:, perm[j]]; for eigh U = R[:, perm[j]].
+template <class T>
+__global__ void __launch_bounds__(256) k_finish_copy(const T *__restrict__ work, const T *__restrict__ rot,
+                                                     double *__restrict__ U, double *__restrict__ V,
+                                                     const double *__restrict__ S, const SectorDesc *__restrict__ secs,
+                                                     const int *__restrict__ perm, const int *__restrict__ dpos) {
+    const SectorDesc sd = secs[blockIdx.y];
+    const int q = sd.q, p = sd.p;
+    const int64_t nw = sd.mode == 1 ? 0 : int64_t(q) * p, n = nw + int64_t(q) * q;
+    const int64_t e0 = int64_t(blockIdx.x) * 2048;
+    if (e0 >= n) return;
+    const T *W = work + sd.w_off;
+    const T *R = rot + sd.rot_off;
+    const int *pm = perm + sd.s_off;
+    double *Wside = sd.trans ? (V + sd.v_off) : (U + sd.u_off);
+    double *Rside = sd.mode == 1 ? (U + sd.u_off) : (sd.trans ? (U + sd.u_off) : (V + sd.v_off));
+    const int64_t e1 = min(n, e0 + 2048);
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        if (e < nw) {
+            const int j = int(e / p), r = int(e - int64_t(j) * p);
+            const double sj = S[sd.s_off + j];
+            const bool zero = !(sj > 0.0) || (dpos && dpos[sd.s_off + j] == 1);
+            Wside[e] = zero ? 0.0 : double(W[int64_t(pm[j]) * p + r]) / sj;
+        } else {
+            const int64_t f = e - nw;
+            const int j = int(f / q), r = int(f - int64_t(j) * q);
+            Rside[f] = double(R[int64_t(pm[j]) * q + r]);
+        }
+    }
 }
 
 int sm_count() {
@@ -1445,7 +1484,8 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
 
 template <class T>
 void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
-                 int max_q, double *scratch, int cap, const T *dnorm, int *dpos, cudaStream_t stream) {
+                 int max_q, double *scratch, int cap, const T *dnorm, int *dpos, int *perm_out, int64_t max_elems,
+                 cudaStream_t stream) {
     size_t smem = size_t(max_q) * (sizeof(double) + 2 * sizeof(int)) + 16;
     static std::once_flag attr;
     std::call_once(attr, [] {
@@ -1453,9 +1493,18 @@ void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, c
                    "finish smem attribute");
     });
     if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the SVD finishing kernel");
-    k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch, cap, dnorm, dpos);
+    // with no null column to complete, the factor writes run on many CTAs per sector
+    const bool split = perm_out && cap == 0 && max_elems > 0;
+    k_finish<T><<<nsec, 1024, smem, stream>>>(work, rot, U, V, s, sec, scratch, cap, dnorm, dpos,
+                                              split ? perm_out : nullptr);
     count_launch();
     cuda_check(cudaGetLastError(), "SVD finishing kernel launch");
+    if (split) {
+        const dim3 grid(unsigned((max_elems + 2047) / 2048), unsigned(nsec));
+        k_finish_copy<T><<<grid, 256, 0, stream>>>(work, rot, U, V, s, sec, perm_out, dpos);
+        count_launch();
+        cuda_check(cudaGetLastError(), "SVD factor copy kernel launch");
+    }
 }
 }  // namespace
 
@@ -1562,19 +1611,21 @@ size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int 
 
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
                       const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap,
-                      const void *dnorm, int *dpos) {
+                      const void *dnorm, int *dpos, int *perm_out, int64_t max_elems) {
     if (nsec <= 0) return;
     if (f32)
         finish_impl(static_cast<const float *>(work), static_cast<const float *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch, complete_cap, static_cast<const float *>(dnorm), dpos, stream);
+                    scratch, complete_cap, static_cast<const float *>(dnorm), dpos, perm_out, max_elems, stream);
     else
         finish_impl(static_cast<const double *>(work), static_cast<const double *>(rot), U, V, s, sec, nsec, max_q,
-                    scratch, complete_cap, static_cast<const double *>(dnorm), dpos, stream);
+                    scratch, complete_cap, static_cast<const double *>(dnorm), dpos, perm_out, max_elems, stream);
 }
 
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec, int nsec,
-                   int max_q, double *scratch, int f32, int complete_cap, const void *dnorm, int *dpos) {
-    launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32, complete_cap, dnorm, dpos);
+                   int max_q, double *scratch, int f32, int complete_cap, const void *dnorm, int *dpos, int *perm_out,
+                   int64_t max_elems) {
+    launch_finish_on(ctx().stream, work, rot, U, V, s, sec, nsec, max_q, scratch, f32, complete_cap, dnorm, dpos,
+                     perm_out, max_elems);
 }
 
 }  // namespace qtt

@@ -208,10 +208,12 @@ size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int 
 // column-major and s (k) per sector in FP64, k = min(m, n).  max_q: largest q;
 // scratch: FP64 buffer with the work buffer's element offsets.  complete_cap >= 0
 // completes only the first complete_cap null columns of each sector (in value
-// order): the caller truncates the others away.
+// order): the caller truncates the others away.  perm_out (sum of q ints at s_off) with
+// complete_cap == 0: the factor writes run on many CTAs per sector (max_elems: the
+// largest q * (p + q) over the sectors).
 void launch_finish(const void *work, const void *rot, double *U, double *V, double *s, const SectorDesc *sec,
                    int nsec, int max_q, double *scratch, int f32, int complete_cap = -1, const void *dnorm = nullptr,
-                   int *dpos = nullptr);
+                   int *dpos = nullptr, int *perm_out = nullptr, int64_t max_elems = 0);
 // The same two launches on an explicit stream (no library context involved).
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
@@ -219,7 +221,8 @@ void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDe
                       const void *defl = nullptr, void *dnorm = nullptr);
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
                       const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap = -1,
-                      const void *dnorm = nullptr, int *dpos = nullptr);
+                      const void *dnorm = nullptr, int *dpos = nullptr, int *perm_out = nullptr,
+                      int64_t max_elems = 0);
 // Segment = one output block (rows x k row-major at dst_off) from a column-major
 // (ld x *) sector matrix at src_off: dst[i*k + j] = src[src_off + (r0 + i) + j*ld].
 struct ScatterEntry {

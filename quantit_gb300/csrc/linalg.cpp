@@ -346,9 +346,16 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
         }
         launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
                       vwork->p, vb, deflate ? thr->p : nullptr, deflate ? dnorm->p : nullptr);
+        BufPtr permbuf;
+        int64_t max_elems = 0;
+        if (cap == 0) {
+            permbuf = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * sizeof(int));
+            for (const SectorDesc &d : D.desc) max_elems = std::max(max_elems, int64_t(d.q) * (d.p + d.q));
+        }
         launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
                       static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32, cap,
-                      deflate ? dnorm->p : nullptr, deflate ? static_cast<int *>(dpos->p) : nullptr);
+                      deflate ? dnorm->p : nullptr, deflate ? static_cast<int *>(dpos->p) : nullptr,
+                      permbuf ? static_cast<int *>(permbuf->p) : nullptr, max_elems);
         if (deflate) {
             // left vectors of the deflated columns: an orthonormal completion (FP32 Householder)
             std::vector<int64_t> coff(nsec);
