@@ -378,6 +378,7 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
         pairs[k].pad = 0;
     }
     std::vector<std::pair<double, GemmTile>> wt;
+    int64_t max_chunks = 0;
     for (int64_t o = 0; o < nout; ++o) {
         int64_t ia = P.pair_a[P.out_p0[o]], ib = P.pair_b[P.out_p0[o]];
         int64_t M = prod_sizes(A, ia, P.freeA), N = prod_sizes(B, ib, P.freeB);
@@ -389,7 +390,13 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
         outs[o].p0 = int32_t(P.out_p0[o]);
         outs[o].p1 = int32_t(P.out_p1[o]);
         double ksum = 0;
-        for (int64_t p = P.out_p0[o]; p < P.out_p1[o]; ++p) ksum += pairs[p].K;
+        int64_t chunks = 0;
+        for (int64_t p = P.out_p0[o]; p < P.out_p1[o]; ++p) {
+            ksum += pairs[p].K;
+            // K chunks of the tensor-core kernels: 32 TF32 (K padded to 8) / 64 BF16 (to 16)
+            chunks += mode == GEMM_BF16X3 ? (((pairs[p].K + 15) & ~15) + 63) / 64 : (((pairs[p].K + 7) & ~7) + 31) / 32;
+        }
+        max_chunks = std::max(max_chunks, chunks);
         flops += 2.0 * double(M) * double(N) * ksum;
         for (int64_t m0 = 0; m0 < M; m0 += TM)
             for (int64_t n0 = 0; n0 < N; n0 += TN)
@@ -434,7 +441,7 @@ void run_contraction(const ContractPlan &P, const BT &A, const BT &B, BT &out, c
         g.outs = douts;
         g.tiles = dtiles;
         g.ntiles = int32_t(tiles.size());
-        g.pad = 0;
+        g.max_chunks = int32_t(std::min<int64_t>(max_chunks, INT32_MAX));
         g.alpha = alpha;
         g.beta = beta;
         launch_gemm_tc(g, mode);

@@ -33,8 +33,7 @@ constexpr int BTMEM_COLS = 128;
 constexpr uint32_t BSBO = (BK * 2 / 16) * 128;     // next 8-row group: 8 core matrices along K (1 KB)
 constexpr int COPY_BYTES = 128 * BK * 2;           // one operand copy (hi, mid or lo): 16 KB
 constexpr int BSTAGE_BYTES = 6 * COPY_BYTES;       // hi/mid/lo of A and B: 96 KB
-constexpr int BNSTAGE = 2;
-constexpr int BSMEM_BYTES = BNSTAGE * BSTAGE_BYTES + 1024;
+constexpr int bsmem_bytes(int nstage) { return nstage * BSTAGE_BYTES + 1024; }
 using tc::LBO;
 
 // no-swizzle K-major descriptor with this kernel's 8-row-group stride
@@ -95,6 +94,7 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
+template <int BNSTAGE>
 __global__ void __launch_bounds__(BTHREADS, 1) k_gemm_bf16x3(TcArgs g, int *err) {
     extern __shared__ __align__(1024) char smem_raw[];
     char *smem = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -283,13 +283,23 @@ void launch_split_bf16x3(const double *src, void *hi, void *mid, void *lo, const
     cuda_check(cudaGetLastError(), "bf16 split kernel launch");
 }
 
-void launch_gemm_bf16x3(const TcArgs &a, int *err, cudaStream_t stream) {
+template <int NST>
+void launch_bf16x3(const TcArgs &a, int *err, cudaStream_t stream) {
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cuda_check(cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, BSMEM_BYTES),
+        cuda_check(cudaFuncSetAttribute(k_gemm_bf16x3<NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        bsmem_bytes(NST)),
                    "tcgen05 bf16 GEMM smem attribute");
     });
-    k_gemm_bf16x3<<<a.ntiles, BTHREADS, BSMEM_BYTES, stream>>>(a, err);
+    k_gemm_bf16x3<NST><<<a.ntiles, BTHREADS, bsmem_bytes(NST), stream>>>(a, err);
+}
+
+void launch_gemm_bf16x3(const TcArgs &a, int *err, cudaStream_t stream) {
+    // tiles of one K chunk: one stage (2 CTAs per SM); otherwise a 2-stage ring
+    if (a.max_chunks == 1)
+        launch_bf16x3<1>(a, err, stream);
+    else
+        launch_bf16x3<2>(a, err, stream);
     count_launch();
     cuda_check(cudaGetLastError(), "tcgen05 bf16 GEMM launch");
 }

@@ -46,8 +46,9 @@ constexpr int TMEM_COLS = 128;  // FP32 accumulator columns (N)
 constexpr int A_BYTES = TBM * TBK * 4;  // one operand copy: 16 KB
 constexpr int B_BYTES = TBN * TBK * 4;  // 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi/lo of A and B: 64 KB
-constexpr int NSTAGE = 3;
-constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024;
+// up to 3 stages; a launch whose tiles need fewer K chunks uses a smaller ring, so that
+// 2 or 3 CTAs share an SM and hide each other's fixed per-tile latency
+constexpr int smem_bytes(int nstage) { return nstage * STAGE_BYTES + 1024; }
 using tc::LBO;
 using tc::SBO;
 using tc::smem_u32;
@@ -119,6 +120,7 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t da, uint64_t db
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
+template <int NSTAGE>
 __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err) {
     extern __shared__ __align__(1024) char smem_raw[];
     char *smem = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -325,6 +327,16 @@ void launch_amax(const double *x, int64_t n, unsigned long long *amax) {
     cuda_check(cudaGetLastError(), "amax kernel launch");
 }
 
+template <int NST>
+void launch_tf32x3(const TcArgs &a) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cuda_check(cudaFuncSetAttribute(k_gemm_tf32x3<NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(NST)),
+                   "tcgen05 GEMM smem attribute");
+    });
+    k_gemm_tf32x3<NST><<<a.ntiles, TTHREADS, smem_bytes(NST), ctx().stream>>>(a, err_word());
+}
+
 void launch_gemm_tc(const TcArgs &a, int mode) {
     if (mode != GEMM_TF32X3 && mode != GEMM_BF16X3) fail(ERR_INVALID_ARGUMENT, "unknown tensor-core GEMM mode");
     if (a.ntiles <= 0) return;
@@ -333,12 +345,13 @@ void launch_gemm_tc(const TcArgs &a, int mode) {
         ctx().tc_used = true;
         return;
     }
-    static std::once_flag attr;
-    std::call_once(attr, [] {
-        cuda_check(cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
-                   "tcgen05 GEMM smem attribute");
-    });
-    k_gemm_tf32x3<<<a.ntiles, TTHREADS, SMEM_BYTES, ctx().stream>>>(a, err_word());
+    const int mc = a.max_chunks;
+    if (mc == 1)
+        launch_tf32x3<1>(a);
+    else if (mc == 2)
+        launch_tf32x3<2>(a);
+    else
+        launch_tf32x3<3>(a);
     count_launch();
     ctx().tc_used = true;
     cuda_check(cudaGetLastError(), "tcgen05 GEMM launch");

@@ -99,7 +99,8 @@ struct TcArgs {
     const GemmPair *pairs;
     const GemmOut *outs;
     const GemmTile *tiles;
-    int32_t ntiles, pad;
+    int32_t ntiles;
+    int32_t max_chunks;  // most K chunks of any tile (sizes the shared-memory ring; 0: unknown)
     double alpha, beta;
 };
 void launch_gemm_tc(const TcArgs &a, int mode);
