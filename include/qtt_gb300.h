@@ -81,6 +81,10 @@ int qtt_autotune_report(char *buf, int64_t cap, int64_t *len);
  * as its singular value, and its left vector is an orthonormal completion of the
  * resolved ones (FP32 Householder).  Fewer sweeps, plus the cost of the completion. */
 int qtt_set_svd_deflation(int on);
+/* Persistent split-TF32 GEMM (one CTA per SM walking the tile list, double-buffered TMEM
+ * accumulator) for launches of at least two tiles per SM; on by default (no reference
+ * counterpart). */
+int qtt_set_persistent_gemm(int on);
 /* Free and total bytes of the calling thread's device (no reference counterpart;
  * the serving loop admits solves against it). */
 int qtt_device_memory(int64_t *free_bytes, int64_t *total_bytes);

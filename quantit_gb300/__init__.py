@@ -32,6 +32,12 @@ def set_svd_deflation(on):
     call("qtt_set_svd_deflation", 1 if on else 0)
 
 
+def set_persistent_gemm(on):
+    """Persistent split-TF32 GEMM for launches of many tiles (on by default)."""
+    from ._lib import call
+    call("qtt_set_persistent_gemm", 1 if on else 0)
+
+
 def autotune_report():
     """The autotuner's decisions, one line per class of decomposition."""
     import ctypes as C

@@ -99,6 +99,9 @@ int qtt_set_autotune(int on) {
 int qtt_set_svd_deflation(int on) {
     return guarded([&] { qtt::set_svd_deflation(on); });
 }
+int qtt_set_persistent_gemm(int on) {
+    return guarded([&] { qtt::set_persistent_gemm(on); });
+}
 int qtt_autotune_report(char *buf, int64_t cap, int64_t *len) {
     return guarded([&] {
         const std::string r = qtt::autotune_report();

@@ -61,6 +61,7 @@ using tc::f32_to_f64_int;
 using tc::mbar_expect_tx;
 using tc::bulk_g2s;
 using tc::umma_commit;
+using tc::mbar_arrive;
 static_assert(SBO == (TBK * 4 / 16) * 128, "the shared layout assumes 128-byte rows per K chunk");
 
 // kind::tf32, D=F32, A=B=TF32, both K-major, N=128, M=128
@@ -295,6 +296,211 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3(TcArgs g, int *err)
     }
 }
 
+// Persistent variant for launches of many tiles: one CTA per SM walks the sorted tile
+// list (tiles blockIdx.x, + gridDim.x, ...).  The producer warp streams the K chunks of
+// its tiles through the ring without draining it between tiles; the MMA thread
+// accumulates tile i in TMEM buffer i % 2 (2 x 128 columns) and commits it to
+// acc_full[i % 2]; warps 4-7 (one TMEM lane quarter each) run tile i's epilogue from
+// that buffer and release it on acc_empty[i % 2] while the MMAs of tile i + 1 proceed.
+template <int NSTAGE>
+__global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3_persistent(TcArgs g, int *err) {
+    extern __shared__ __align__(1024) char smem_raw[];
+    char *smem = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ uint64_t full[NSTAGE], empty[NSTAGE], acc_full[2], acc_empty[2];
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ int n_issued, n_consumed;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                     "r"(2 * TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        n_issued = 0;
+        n_consumed = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base_sh;
+    auto tile_chunks = [&](const GemmOut &o) {
+        int n = 0;
+        for (int p = o.p0; p < o.p1; ++p) n += (((g.pairs[p].K + 7) & ~7) + TBK - 1) / TBK;
+        return n;
+    };
+
+    if (warp == 0) {
+        const float *srcs[4] = {static_cast<const float *>(g.Ahi), static_cast<const float *>(g.Alo),
+                                static_cast<const float *>(g.Bhi), static_cast<const float *>(g.Blo)};
+        int gc = 0;
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < g.ntiles && !stop; tile += gridDim.x) {
+            const GemmTile t = g.tiles[tile];
+            const GemmOut o = g.outs[t.out];
+            const int rga = min(TBM / 8, (o.M - t.m0 + 7) / 8), rgb = min(TBN / 8, (o.N - t.n0 + 7) / 8);
+            const int nch = tile_chunks(o);
+            int p = o.p0, k0 = 0;
+            for (int c = 0; c < nch; ++c) {
+                const int s = gc % NSTAGE;
+                int ok = 1;
+                if (lane == 0 && gc >= NSTAGE) ok = mbar_wait(&empty[s], ((gc / NSTAGE) - 1) & 1) ? 1 : 0;
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (!ok) {
+                    if (lane == 0) atomicExch(err, 1);
+                    stop = true;
+                    break;
+                }
+                while (k0 >= ((g.pairs[p].K + 7) & ~7)) {
+                    ++p;
+                    k0 = 0;
+                }
+                const GemmPair pr = g.pairs[p];
+                const int KP = (pr.K + 7) & ~7, kv = min(TBK, KP - k0);
+                const uint32_t rg_bytes = uint32_t(kv) * 32u;
+                if (lane == 0) mbar_expect_tx(&full[s], 2u * rg_bytes * uint32_t(rga + rgb));
+                __syncwarp();
+                char *st = smem + s * STAGE_BYTES;
+                const int nA = 2 * rga, ncopy = 2 * (rga + rgb);
+                for (int i = lane; i < ncopy; i += 32) {
+                    const bool isA = i < nA;
+                    const int j = isA ? i : i - nA, which = j & 1, rg = j >> 1;
+                    const int64_t grg = (isA ? t.m0 : t.n0) / 8 + rg;
+                    const float *src = srcs[(isA ? 0 : 2) + which] + (isA ? pr.a_off : pr.b_off) +
+                                       (grg * (KP / 4) + k0 / 4) * 32;
+                    char *dst = st + (isA ? 0 : 2 * A_BYTES) + which * (isA ? A_BYTES : B_BYTES) + rg * int(SBO);
+                    bulk_g2s(dst, src, rg_bytes, &full[s]);
+                }
+                k0 += TBK;
+                ++gc;
+            }
+        }
+        if (lane == 0) n_issued = gc;
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = idesc_tf32();
+        int gc = 0, i = 0;
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < g.ntiles && !stop; tile += gridDim.x, ++i) {
+            const GemmOut o = g.outs[g.tiles[tile].out];
+            const int b = i & 1;
+            if (i >= 2 && !mbar_wait(&acc_empty[b], ((i / 2) - 1) & 1)) {
+                atomicExch(err, 2);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t acc_t = tmem + uint32_t(b * TMEM_COLS);
+            const int nch = tile_chunks(o);
+            int p = o.p0, k0 = 0;
+            for (int c = 0; c < nch; ++c) {
+                const int s = gc % NSTAGE;
+                if (!mbar_wait(&full[s], (gc / NSTAGE) & 1)) {
+                    atomicExch(err, 2);
+                    stop = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                while (k0 >= ((g.pairs[p].K + 7) & ~7)) {
+                    ++p;
+                    k0 = 0;
+                }
+                const int kv = min(TBK, ((g.pairs[p].K + 7) & ~7) - k0);
+                char *st = smem + s * STAGE_BYTES;
+                const uint32_t a_hi = smem_u32(st), a_lo = a_hi + A_BYTES, b_hi = a_hi + 2 * A_BYTES,
+                               b_lo = b_hi + B_BYTES;
+                for (int ks = 0; ks < kv / 8; ++ks) {
+                    const uint32_t koff = uint32_t(ks) * 2u * LBO;
+                    const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
+                    mma_tf32(acc_t, make_desc(a_hi + koff), make_desc(b_lo + koff), idesc, acc0);
+                    mma_tf32(acc_t, make_desc(a_lo + koff), make_desc(b_hi + koff), idesc, 1u);
+                    mma_tf32(acc_t, make_desc(a_hi + koff), make_desc(b_hi + koff), idesc, 1u);
+                }
+                umma_commit(&empty[s]);
+                k0 += TBK;
+                ++gc;
+            }
+            umma_commit(&acc_full[b]);  // this tile's accumulator is final once its MMAs complete
+        }
+        n_consumed = gc;
+    } else if (warp >= 4) {
+        // epilogue: warp 4 + q reads TMEM lanes 32 q .. 32 q + 31 (rows), all 128 columns
+        const int quarter = warp - 4;
+        const int shift = amax_shift(*g.amax_a) + amax_shift(*g.amax_b);
+        const int row = quarter * 32 + lane;
+        int i = 0;
+        for (int tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++i) {
+            const GemmTile t = g.tiles[tile];
+            const GemmOut o = g.outs[t.out];
+            const int b = i & 1;
+            int ok = 1;
+            if (lane == 0) ok = mbar_wait(&acc_full[b], (i / 2) & 1) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                if (lane == 0) atomicExch(err, 2);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const bool have_acc = tile_chunks(o) > 0;
+            const int gm = t.m0 + row;
+            const bool plain = g.alpha == 1.0 && o.add_off < 0;
+#pragma unroll 1
+            for (int cb = 0; cb < 4; ++cb) {
+                const int col0 = cb * 32;
+                uint32_t v[32];
+                const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b * TMEM_COLS + col0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (gm < o.M) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int gn = t.n0 + col0 + j;
+                        if (gn < o.N) {
+                            const int64_t idx = int64_t(gm) * o.N + gn;
+                            double val = have_acc ? f32_to_f64_int(__uint_as_float(v[j]), shift) : 0.0;
+                            if (!plain) {
+                                val *= g.alpha;
+                                if (o.add_off >= 0) val += g.beta * g.Cadd[o.add_off + idx];
+                            }
+                            g.C[o.c_off + idx] = val;
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // copies issued but never consumed (only after a timeout) must land before exit
+        for (int c = n_consumed; c < n_issued; ++c)
+            if (!mbar_wait(&full[c % NSTAGE], (c / NSTAGE) & 1)) atomicExch(err, 2);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TMEM_COLS));
+    }
+}
+
 // the calling thread's error word (one per stream context, so concurrent solves
 // on different threads see only their own kernels' status)
 int *err_word() {
@@ -327,6 +533,28 @@ void launch_amax(const double *x, int64_t n, unsigned long long *amax) {
     cuda_check(cudaGetLastError(), "amax kernel launch");
 }
 
+int tc_sm_count() {
+    static std::once_flag once;
+    static int nsm = 0;
+    std::call_once(once, [] {
+        int dev = 0;
+        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    });
+    return nsm;
+}
+
+void launch_tf32x3_persistent(const TcArgs &a) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cuda_check(cudaFuncSetAttribute(k_gemm_tf32x3_persistent<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        smem_bytes(3)),
+                   "tcgen05 persistent GEMM smem attribute");
+    });
+    const int grid = std::min(a.ntiles, tc_sm_count());
+    k_gemm_tf32x3_persistent<3><<<grid, TTHREADS, smem_bytes(3), ctx().stream>>>(a, err_word());
+}
+
 template <int NST>
 void launch_tf32x3(const TcArgs &a) {
     static std::once_flag attr;
@@ -346,7 +574,9 @@ void launch_gemm_tc(const TcArgs &a, int mode) {
         return;
     }
     const int mc = a.max_chunks;
-    if (mc == 1)
+    if (a.ntiles >= 2 * tc_sm_count() && persistent_gemm())
+        launch_tf32x3_persistent(a);
+    else if (mc == 1)
         launch_tf32x3<1>(a);
     else if (mc == 2)
         launch_tf32x3<2>(a);

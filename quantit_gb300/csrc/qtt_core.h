@@ -330,6 +330,9 @@ int jacobi_variant();
 // Block-width autotuner of the block-Jacobi kernel (on by default) and its decisions.
 void set_autotune(int on);
 std::string autotune_report();
+// Persistent tensor-core GEMM for launches of at least two tiles per SM (on by default).
+void set_persistent_gemm(int on);
+int persistent_gemm();
 // Deflation of numerically zero columns in the FP32 SVD of a truncating svd (off by default).
 void set_svd_deflation(int on);
 int svd_deflation();

@@ -61,6 +61,11 @@ static __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint
         : "memory");
 }
 
+// Plain arrival on an mbarrier.
+static __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // Commit the calling thread's prior tcgen05.mma operations to an mbarrier (one arrival
 // when they have completed).
 static __device__ __forceinline__ void umma_commit(uint64_t *bar) {

@@ -131,3 +131,34 @@ def test_mixed_dmrg_from_noncanonical_state():
     for gemm in TC_MODES:
         assert np.isfinite(out[gemm])
         assert abs(out[gemm] - out["f64"]) / L < 1e-7, (gemm, out)
+
+
+def test_persistent_gemm_matches_one_tile_per_cta():
+    """Launches of at least two tiles per SM run the persistent kernel (one CTA per SM
+    walking the tile list, double-buffered TMEM accumulator).  Each tile's MMA sequence
+    is the same as in the one-tile-per-CTA kernel, so the results are identical, and
+    they match FP64 products to FP32 accuracy."""
+    from quantit_gb300.conserved import Z
+    rng = np.random.default_rng(25)
+    ns, m, k = 9, 700, 300  # 9 output blocks of 700 x 700: 324 tiles of 128 x 128
+    A = q.btensor([[(m, Z(i)) for i in range(ns)], [(k, Z(-i)) for i in range(ns)]], Z(0))
+    B = q.btensor([[(k, Z(i)) for i in range(ns)], [(m, Z(-i)) for i in range(ns)]], Z(0))
+    a_blocks = [((i, i), rng.standard_normal((m, k))) for i in range(ns)]
+    b_blocks = [((i, i), rng.standard_normal((k, m))) for i in range(ns)]
+    A.set_blocks(a_blocks)
+    B.set_blocks(b_blocks)
+    out = {}
+    q.set_gemm_mode("tf32x3")
+    try:
+        for persistent in (False, True):
+            q.set_persistent_gemm(persistent)
+            out[persistent] = dict(A.tensordot(B, ([1], [0])).blocks())
+    finally:
+        q.set_persistent_gemm(True)
+        q.set_gemm_mode("f64")
+    assert out[True].keys() == out[False].keys()
+    for key in out[False]:
+        np.testing.assert_array_equal(out[True][key], out[False][key])
+    for (key, a), (_, b) in zip(a_blocks, b_blocks):
+        want = a @ b
+        assert float(np.max(np.abs(out[True][key] - want))) <= TOL * float(np.max(np.abs(want))) * 4
