@@ -133,7 +133,8 @@ def test_mixed_dmrg_from_noncanonical_state():
         assert abs(out[gemm] - out["f64"]) / L < 1e-7, (gemm, out)
 
 
-def test_persistent_gemm_matches_one_tile_per_cta():
+@pytest.mark.parametrize("mode", TC_MODES)
+def test_persistent_gemm_matches_one_tile_per_cta(mode):
     """Launches of at least two tiles per SM run the persistent kernel (one CTA per SM
     walking the tile list, double-buffered TMEM accumulator).  Each tile's MMA sequence
     is the same as in the one-tile-per-CTA kernel, so the results are identical, and
@@ -148,7 +149,7 @@ def test_persistent_gemm_matches_one_tile_per_cta():
     A.set_blocks(a_blocks)
     B.set_blocks(b_blocks)
     out = {}
-    q.set_gemm_mode("tf32x3")
+    q.set_gemm_mode(mode)
     try:
         for persistent in (False, True):
             q.set_persistent_gemm(persistent)
