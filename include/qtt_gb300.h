@@ -81,7 +81,7 @@ int qtt_autotune_report(char *buf, int64_t cap, int64_t *len);
  * as its singular value, and its left vector is an orthonormal completion of the
  * resolved ones (FP32 Householder).  Fewer sweeps, plus the cost of the completion. */
 int qtt_set_svd_deflation(int on);
-/* Persistent split-TF32 GEMM (one CTA per SM walking the tile list, double-buffered TMEM
+/* Persistent split-TF32 / split-BF16 GEMMs (one CTA per SM walking the tile list, double-buffered TMEM
  * accumulator) for launches of at least two tiles per SM; on by default (no reference
  * counterpart). */
 int qtt_set_persistent_gemm(int on);
