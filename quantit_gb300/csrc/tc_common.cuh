@@ -2,8 +2,9 @@
 // split-BF16): shared-memory addresses and UMMA descriptors of the canonical
 // no-swizzle K-major layout (rows of 128 bytes per K chunk: core matrices of
 // 8 rows x 16 bytes, LBO = 128 B to the next core matrix along K, SBO = 1024 B to
-// the next 8-row group), bounded mbarrier waits, 16-byte shared stores, the
-// operands' power-of-two scaling and the integer FP64 <-> FP32 conversions.
+// the next 8-row group), bounded mbarrier waits, mbarrier arrivals and transaction
+// counts, bulk asynchronous global -> shared copies, MMA commits, the operands'
+// power-of-two scaling and the integer FP64 <-> FP32 conversions.
 #pragma once
 #include <cstdint>
 
@@ -130,12 +131,6 @@ static __device__ __forceinline__ double f32_to_f64_int(float f, int shift) {
             d = sign | ((unsigned long long)de << 52) | ((unsigned long long)m << 29);
     }
     return __longlong_as_double(static_cast<long long>(d));
-}
-
-static __device__ __forceinline__ void st_shared_v4(char *p, uint4 v) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(smem_u32(p)), "r"(v.x), "r"(v.y), "r"(v.z),
-                 "r"(v.w)
-                 : "memory");
 }
 
 }  // namespace tc
