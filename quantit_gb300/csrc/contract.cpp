@@ -302,6 +302,14 @@ void split_operand(const BT &t, const std::vector<int64_t> &perm, int nrow, std:
         e.rank = r;
         e.K = int32_t(K);
         e.K4 = int32_t(K4);
+        // index-math fast paths of the split kernels
+        bool contig = true;
+        int64_t sfx = 1;
+        for (int i = r - 1; i >= 0; --i) {
+            if (e.stride[i] != sfx && e.dims[i] != 1) contig = false;
+            sfx *= e.dims[i];
+        }
+        e.flags = (rows * K < int64_t(INT32_MAX) ? SPLIT_SMALL : 0) | (contig ? SPLIT_CONTIG : 0);
         offs[b] = o;
         lens[b] = rows * K;
         o += ((rows + 7) & ~int64_t(7)) * K4;

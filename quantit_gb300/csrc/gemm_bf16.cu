@@ -63,23 +63,16 @@ __global__ void k_split_bf16x3(const double *__restrict__ src, uint16_t *__restr
                                const Chunk *__restrict__ chunks, const unsigned long long *__restrict__ amax) {
     const Chunk ch = chunks[blockIdx.x];
     const SplitEntry &e = ents[ch.seg];
-    const int r = e.rank;
     const int shift = tc::amax_shift(*amax);
     for (int i = threadIdx.x; i < ch.len; i += blockDim.x) {
         const int64_t lin = ch.start + i;
-        int64_t rem = lin, so = e.src_off;
-        for (int d = r - 1; d >= 0; --d) {
-            const int64_t n = e.dims[d];
-            const int64_t q = rem / n;
-            so += (rem - q * n) * e.stride[d];
-            rem = q;
-        }
-        const float x = tc::f64_to_f32_int(src[so], shift);
+        const float x = tc::f64_to_f32_int(src[split_src(e, lin)], shift);
         const uint16_t h = to_bf16(x);
         const float r1 = x - from_bf16(h);
         const uint16_t m = to_bf16(r1);
         const uint16_t l = to_bf16(r1 - from_bf16(m));
-        const int64_t row = lin / e.K, k = lin - row * e.K;
+        int64_t row, k;
+        split_rowk(e, lin, row, k);
         const int64_t dst = e.dst_off + ((row >> 3) * (e.K4 >> 3) + (k >> 3)) * 64 + (row & 7) * 8 + (k & 7);
         hi[dst] = h;
         mid[dst] = m;

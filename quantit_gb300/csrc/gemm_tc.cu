@@ -93,21 +93,14 @@ __global__ void k_split_tf32(const double *__restrict__ src, float *__restrict__
                              const unsigned long long *__restrict__ amax) {
     const Chunk ch = chunks[blockIdx.x];
     const SplitEntry &e = ents[ch.seg];
-    const int r = e.rank;
     const int shift = amax_shift(*amax);
     for (int i = threadIdx.x; i < ch.len; i += blockDim.x) {
         const int64_t lin = ch.start + i;
-        int64_t rem = lin, so = e.src_off;
-        for (int d = r - 1; d >= 0; --d) {
-            const int64_t n = e.dims[d];
-            const int64_t q = rem / n;
-            so += (rem - q * n) * e.stride[d];
-            rem = q;
-        }
-        const float xf = f64_to_f32_int(src[so], shift);
+        const float xf = f64_to_f32_int(src[split_src(e, lin)], shift);
         const uint32_t h = to_tf32(xf);
         const uint32_t l = to_tf32(xf - __uint_as_float(h));
-        const int64_t row = lin / e.K, k = lin - row * e.K;
+        int64_t row, k;
+        split_rowk(e, lin, row, k);
         const int64_t dst = e.dst_off + ((row >> 3) * (e.K4 >> 2) + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3);
         hi[dst] = __uint_as_float(h);
         lo[dst] = __uint_as_float(l);

@@ -73,10 +73,43 @@ struct SplitEntry {
     // K4: the padded K (rounded up to 8 for TF32X3, 16 for BF16X3); blocks are tiled in
     // core matrices of 8 rows x 16 bytes (rows padded to 8), a row group's core
     // matrices in K order
-    int32_t rank, K, K4, pad;
+    int32_t rank, K, K4;
+    int32_t flags;  // SPLIT_SMALL: rows * K < 2^31 (32-bit index math); SPLIT_CONTIG: row-major source
     int64_t dims[8];
     int64_t stride[8];
 };
+enum : int32_t { SPLIT_SMALL = 1, SPLIT_CONTIG = 2 };
+// Source offset of element `lin` (row-major over dims) of a split entry.
+__device__ __forceinline__ int64_t split_src(const SplitEntry &e, int64_t lin) {
+    if (e.flags & SPLIT_CONTIG) return e.src_off + lin;
+    if (e.flags & SPLIT_SMALL) {
+        uint32_t rem = uint32_t(lin), off = 0;
+        for (int d = e.rank - 1; d >= 0; --d) {
+            const uint32_t n = uint32_t(e.dims[d]), q = rem / n;
+            off += (rem - q * n) * uint32_t(e.stride[d]);
+            rem = q;
+        }
+        return e.src_off + off;
+    }
+    int64_t rem = lin, so = e.src_off;
+    for (int d = e.rank - 1; d >= 0; --d) {
+        const int64_t n = e.dims[d], q = rem / n;
+        so += (rem - q * n) * e.stride[d];
+        rem = q;
+    }
+    return so;
+}
+// (row, k) of element `lin` of a split entry's rows x K matrix.
+__device__ __forceinline__ void split_rowk(const SplitEntry &e, int64_t lin, int64_t &row, int64_t &k) {
+    if (e.flags & SPLIT_SMALL) {
+        const uint32_t r = uint32_t(lin) / uint32_t(e.K);
+        row = r;
+        k = int64_t(uint32_t(lin) - r * uint32_t(e.K));
+    } else {
+        row = lin / e.K;
+        k = lin - row * e.K;
+    }
+}
 // amax: the bit pattern of max |x| over the operand (launch_amax); every element is
 // scaled by the exact power of two 2^-ilogb(amax) before the split, so operands of any
 // magnitude use the FP32 range, and the GEMM epilogue undoes the two scales exactly.
