@@ -303,6 +303,12 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3_persistent(TcArgs g
     __shared__ uint32_t tmem_base_sh;
     __shared__ int n_issued, n_consumed;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // round r of the longest-first tile list, in boustrophedon order across the CTAs, so
+    // that every CTA's tiles add up to about the same work
+    auto snake_tile = [&](int r) {
+        const int G = int(gridDim.x), b = int(blockIdx.x);
+        return r * G + ((r & 1) ? (G - 1 - b) : b);
+    };
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
@@ -337,7 +343,9 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3_persistent(TcArgs g
                                 static_cast<const float *>(g.Bhi), static_cast<const float *>(g.Blo)};
         int gc = 0;
         bool stop = false;
-        for (int tile = blockIdx.x; tile < g.ntiles && !stop; tile += gridDim.x) {
+        for (int r = 0; r * int(gridDim.x) < g.ntiles && !stop; ++r) {
+            const int tile = snake_tile(r);
+            if (tile >= g.ntiles) continue;
             const GemmTile t = g.tiles[tile];
             const GemmOut o = g.outs[t.out];
             const int rga = min(TBM / 8, (o.M - t.m0 + 7) / 8), rgb = min(TBN / 8, (o.N - t.n0 + 7) / 8);
@@ -382,7 +390,9 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3_persistent(TcArgs g
         const uint32_t idesc = idesc_tf32();
         int gc = 0, i = 0;
         bool stop = false;
-        for (int tile = blockIdx.x; tile < g.ntiles && !stop; tile += gridDim.x, ++i) {
+        for (int r = 0; r * int(gridDim.x) < g.ntiles && !stop; ++r) {
+            const int tile = snake_tile(r);
+            if (tile >= g.ntiles) continue;
             const GemmOut o = g.outs[g.tiles[tile].out];
             const int b = i & 1;
             if (i >= 2 && !mbar_wait(&acc_empty[b], ((i / 2) - 1) & 1)) {
@@ -421,6 +431,7 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3_persistent(TcArgs g
                 ++gc;
             }
             umma_commit(&acc_full[b]);  // this tile's accumulator is final once its MMAs complete
+            ++i;
         }
         n_consumed = gc;
     } else if (warp >= 4) {
@@ -429,7 +440,9 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3_persistent(TcArgs g
         const int shift = amax_shift(*g.amax_a) + amax_shift(*g.amax_b);
         const int row = quarter * 32 + lane;
         int i = 0;
-        for (int tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++i) {
+        for (int r = 0; r * int(gridDim.x) < g.ntiles; ++r) {
+            const int tile = snake_tile(r);
+            if (tile >= g.ntiles) continue;
             const GemmTile t = g.tiles[tile];
             const GemmOut o = g.outs[t.out];
             const int b = i & 1;
@@ -478,6 +491,7 @@ __global__ void __launch_bounds__(TTHREADS, 1) k_gemm_tf32x3_persistent(TcArgs g
             asm volatile("tcgen05.fence::before_thread_sync;");
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[b]);
+            ++i;
         }
     }
     __syncthreads();
