@@ -1447,7 +1447,11 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
                     TuneState &st = g_tune[key];
                     st.tried[ci] += 1;
                     st.best_ms[ci] = std::min(st.best_ms[ci], ms);
-                    if (st.winner < 0 && st.tried[0] >= TUNE_TRIALS && st.tried[1] >= TUNE_TRIALS) {
+                    // decide after TUNE_TRIALS of each width, or as soon as one trial of each
+                    // shows a clear gap (> 1.5x and > 2 ms, beyond any first-launch cost)
+                    const float lo = std::min(st.best_ms[0], st.best_ms[1]), hi = std::max(st.best_ms[0], st.best_ms[1]);
+                    const bool clear = st.tried[0] >= 1 && st.tried[1] >= 1 && hi > 1.5f * lo && hi - lo > 2.0f;
+                    if (st.winner < 0 && (clear || (st.tried[0] >= TUNE_TRIALS && st.tried[1] >= TUNE_TRIALS))) {
                         st.winner = st.best_ms[1] < st.best_ms[0] ? 1 : 0;
                         tune_save(key, st.winner);
                     }
