@@ -229,3 +229,24 @@ def test_reshape_as_acceptance_matches_oracle(mods):
             assert (want is None) == (got is None), (legs, lv, want, got)
             n += 1
     assert n > 50
+
+
+def test_tuning_switches_and_dmrg_options_round_trip():
+    """The tuning switches with no reference counterpart (persistent GEMM, SVD deflation,
+    autotuner, Jacobi kernel) are plain host settings: they take effect without a GPU, and
+    dmrg_options carries the build's extra fields into the C struct unchanged."""
+    import quantit_gb300 as q
+    for on in (False, True):
+        q.set_persistent_gemm(on)
+        q.set_svd_deflation(on)
+        q.set_autotune(on)
+    q.set_svd_deflation(False)
+    for kernel in ("scalar", "block"):
+        q.set_jacobi_kernel(kernel)
+    with pytest.raises(ValueError):
+        q.set_jacobi_kernel(7)
+    o = q.algorithms.dmrg_options(gemm="bf16x3", lanczos_steps=4, cuda_graphs=False, svd_warm_start=False,
+                                  final_energy_fp64=False)._c()
+    assert (o.gemm_mode, o.lanczos_steps, o.cuda_graphs, o.svd_warm_start, o.final_energy_fp64) == (2, 4, 0, 0, 0)
+    d = q.algorithms.dmrg_options()._c()
+    assert (d.gemm_mode, d.lanczos_steps, d.cuda_graphs, d.svd_warm_start, d.final_energy_fp64) == (0, 1, 1, 1, 1)
