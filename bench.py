@@ -606,7 +606,12 @@ def main():
             "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e}
     if cmp:
         line["vs_fp64"] = cmp
-    line["autotune"] = q.autotune_report().splitlines()
+    # the autotuner's decisions go to stderr: one line each would push the metric keys
+    # out of the tail a log reader keeps
+    tune = q.autotune_report().splitlines()
+    line["autotune_classes"] = len(tune)
+    if rank == 0:
+        print("autotune:\n  " + "\n  ".join(tune), file=sys.stderr)
     if rank == 0 and not args.no_cpu_baseline and (hub or cyl):
         line["cpu_baseline"] = None  # the oracle sampler restates the Heisenberg bond update only
     elif rank == 0 and not args.no_cpu_baseline:

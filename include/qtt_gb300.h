@@ -227,18 +227,23 @@ int qtt_mps_energy(int32_t L, const qtt_bt *mpo, const qtt_bt *mps, double *ener
 
 /* ------------------------------------------------------------------ allocation-free SVD
  * No counterpart in QuantiT: an addition for callers that cannot allocate device
- * memory (inside a captured graph region, under a fixed memory budget, or when
- * only pre-registered buffers may be used).  Thin SVD A = U diag(s) V^T of one
- * dense FP64 matrix with the same one-sided Jacobi kernels as the sector SVD,
- * using only a file-scope device array of QTT_SVD_NOALLOC_SCRATCH_BYTES (held by
- * every GPU that loads the library until exit) -- no cudaMalloc / cudaFree.
+ * memory -- a plug-in inside a host application that owns all device memory, a
+ * solver under a memory budget fixed at start-up, or a real-time loop that cannot
+ * afford cudaMalloc / cudaFree (which can synchronise the whole device).
+ * Thin SVD A = U diag(s) V^T of one dense FP64 matrix with the same one-sided
+ * Jacobi kernels as the sector SVD, using only a file-scope device array of
+ * QTT_SVD_NOALLOC_SCRATCH_BYTES (held by every GPU that loads the library until
+ * exit) -- no cudaMalloc / cudaFree and no allocating library routine.
  *   a: m x n row-major (device), u: m x k row-major, s: k, v: n x k row-major
  *   (device outputs), k = min(m, n), m and n <= QTT_SVD_NOALLOC_MAX_DIM; larger
  *   sizes are rejected with QTT_ERR_INVALID_ARGUMENT.  Work is issued on `stream`
- *   (a cudaStream_t, NULL = legacy default stream) and is asynchronous.
- * The first call on a device looks up the scratch array's device address; make
- * that first call outside any stream capture.  All calls share the array: calls
- * whose work overlaps on the GPU race and corrupt each other's results. */
+ *   (a cudaStream_t, NULL = legacy default stream); the call returns without
+ *   waiting for it.
+ * The first call on a device (with that device current) looks up the scratch
+ * array's device address and sets the kernels' attributes for that device; make
+ * that first call before any stream capture.  All calls share the array, which
+ * keeps the last call's contents: calls whose work overlaps on the GPU race and
+ * corrupt each other's results. */
 #define QTT_SVD_NOALLOC_MAX_DIM 256
 #define QTT_SVD_NOALLOC_SCRATCH_BYTES (5u * 256u * 256u * 8u + 2048u)
 int qtt_svd_dense_noalloc(const double *a, int64_t m, int64_t n, double *u, double *s, double *v, void *stream);

@@ -498,8 +498,8 @@ void launch_split_bf16x3(const double *src, void *hi, void *mid, void *lo, const
 
 template <int NST>
 void launch_bf16x3(const TcArgs &a, int *err, cudaStream_t stream) {
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    static std::atomic<uint64_t> attr{0};
+    once_per_device(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_gemm_bf16x3<NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         bsmem_bytes(NST)),
                    "tcgen05 bf16 GEMM smem attribute");
@@ -507,21 +507,12 @@ void launch_bf16x3(const TcArgs &a, int *err, cudaStream_t stream) {
     k_gemm_bf16x3<NST><<<a.ntiles, BTHREADS, bsmem_bytes(NST), stream>>>(a, err);
 }
 
-int bf_sm_count() {
-    static std::once_flag once;
-    static int nsm = 0;
-    std::call_once(once, [] {
-        int dev = 0;
-        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
-    });
-    return nsm;
-}
+int bf_sm_count() { return device_sm_count(); }
 
 void launch_gemm_bf16x3(const TcArgs &a, int *err, cudaStream_t stream) {
     if (a.ntiles >= 2 * bf_sm_count() && persistent_gemm()) {
-        static std::once_flag attr;
-        std::call_once(attr, [] {
+        static std::atomic<uint64_t> attr{0};
+        once_per_device(attr, [] {
             cuda_check(cudaFuncSetAttribute(k_gemm_bf16x3_persistent<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             bsmem_bytes(2)),
                        "tcgen05 persistent bf16 GEMM smem attribute");

@@ -540,20 +540,11 @@ void launch_amax(const double *x, int64_t n, unsigned long long *amax) {
     cuda_check(cudaGetLastError(), "amax kernel launch");
 }
 
-int tc_sm_count() {
-    static std::once_flag once;
-    static int nsm = 0;
-    std::call_once(once, [] {
-        int dev = 0;
-        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
-    });
-    return nsm;
-}
+int tc_sm_count() { return device_sm_count(); }
 
 void launch_tf32x3_persistent(const TcArgs &a) {
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    static std::atomic<uint64_t> attr{0};
+    once_per_device(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_gemm_tf32x3_persistent<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         smem_bytes(3)),
                    "tcgen05 persistent GEMM smem attribute");
@@ -564,8 +555,8 @@ void launch_tf32x3_persistent(const TcArgs &a) {
 
 template <int NST>
 void launch_tf32x3(const TcArgs &a) {
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    static std::atomic<uint64_t> attr{0};
+    once_per_device(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_gemm_tf32x3<NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(NST)),
                    "tcgen05 GEMM smem attribute");
     });

@@ -1202,23 +1202,14 @@ __global__ void __launch_bounds__(256) k_finish_copy(const T *__restrict__ work,
     }
 }
 
-int sm_count() {
-    static std::once_flag once;
-    static int nsm = 0;
-    std::call_once(once, [] {
-        int dev = 0;
-        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-        cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
-    });
-    return nsm;
-}
+int sm_count() { return device_sm_count(); }
 
 // Cooperative grids are sized to the work (pairs or block pairs per step), not to
 // the whole GPU, so that small decompositions on concurrent streams overlap.
 template <class T, int R>
 void jacobi_launch(const JacobiParams<T> &P, size_t smem, int64_t pairs_bound, cudaStream_t stream) {
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    static std::atomic<uint64_t> attr{0};
+    once_per_device(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_jacobi<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024),
                    "Jacobi smem attribute");
     });
@@ -1253,8 +1244,8 @@ bool bjacobi_launch(const BJacobiParams<T> &P, int max_block_steps, int64_t sum_
                     cudaStream_t stream) {
     const size_t smem = size_t(2 * B) * (32 * R + 2 * B + 1) * sizeof(T) + size_t(3 * P.nsec + 1) * sizeof(int);
     if (smem > BJ_SMEM_MAX) return false;
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    static std::atomic<uint64_t> attr{0};
+    once_per_device(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_bjacobi<T, B, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(BJ_SMEM_MAX)),
                    "block Jacobi smem attribute");
@@ -1394,7 +1385,7 @@ void tune_save(const TuneKey &k, int w) {
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
                  int max_sweeps, int *sweeps_out, int *flags, int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes,
-                 const T *defl, T *dnorm, cudaStream_t stream) {
+                 const T *defl, T *dnorm, cudaStream_t stream, bool tune) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
@@ -1423,7 +1414,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
                 TuneState &st = g_tune[key];
                 if (st.winner >= 0 && st.winner < int(cands.size())) {
                     ci = st.winner;
-                } else {
+                } else if (tune) {
                     ci = st.tried[1] < st.tried[0] ? 1 : 0;
                     timing = true;
                 }
@@ -1491,8 +1482,8 @@ void finish_impl(const T *work, const T *rot, double *U, double *V, double *s, c
                  int max_q, double *scratch, int cap, const T *dnorm, int *dpos, int *perm_out, int64_t max_elems,
                  cudaStream_t stream) {
     size_t smem = size_t(max_q) * (sizeof(double) + 2 * sizeof(int)) + 16;
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    static std::atomic<uint64_t> attr{0};
+    once_per_device(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_finish<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
                    "finish smem attribute");
     });
@@ -1535,17 +1526,18 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
-                      int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm) {
+                      int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm,
+                      bool tune) {
     if (nsec <= 0) return;
     if ((defl == nullptr) != (dnorm == nullptr)) fail(ERR_INVALID_ARGUMENT, "deflation needs thresholds and norms");
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
                     max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
-                    static_cast<const float *>(defl), static_cast<float *>(dnorm), stream);
+                    static_cast<const float *>(defl), static_cast<float *>(dnorm), stream, tune);
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
                     max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
-                    static_cast<const double *>(defl), static_cast<double *>(dnorm), stream);
+                    static_cast<const double *>(defl), static_cast<double *>(dnorm), stream, tune);
 }
 
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
@@ -1580,8 +1572,8 @@ void launch_complete_deflated(double *U, double *V, const SectorDesc *sec, int n
     if (nsec <= 0) return;
     const size_t smem = size_t(max_q) * 3 * sizeof(int);
     if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the completion kernel");
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    static std::atomic<uint64_t> attr{0};
+    once_per_device(attr, [] {
         cuda_check(cudaFuncSetAttribute(k_complete_deflated, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
                    "completion smem attribute");
     });

@@ -249,10 +249,12 @@ void launch_finish(const void *work, const void *rot, double *U, double *V, doub
                    int nsec, int max_q, double *scratch, int f32, int complete_cap = -1, const void *dnorm = nullptr,
                    int *dpos = nullptr, int *perm_out = nullptr, int64_t max_elems = 0);
 // The same two launches on an explicit stream (no library context involved).
+// tune == false never times block widths (no host synchronisation): the width the
+// autotuner settled on for the class is used if there is one, else the default.
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
                       int max_p, int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0,
-                      const void *defl = nullptr, void *dnorm = nullptr);
+                      const void *defl = nullptr, void *dnorm = nullptr, bool tune = true);
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
                       const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap = -1,
                       const void *dnorm = nullptr, int *dpos = nullptr, int *perm_out = nullptr,

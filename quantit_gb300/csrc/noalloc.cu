@@ -1,18 +1,26 @@
 // Dense SVD without any device allocation: qtt_svd_dense_noalloc.
 //
-// Some callers cannot call cudaMalloc: code running inside a captured CUDA
-// graph region or a stream-ordered pipeline that must not synchronise the
-// allocator, hosts whose memory budget is fixed up front (embedded solvers,
-// plug-ins loaded into another application's process), or callers that hand
-// the library only pre-registered buffers.  For them this entry point runs the
-// same FP64 one-sided Jacobi as the block-sparse SVD on one dense matrix with
-// all its working storage in a file-scope device array instead of allocations.
+// Some callers cannot call cudaMalloc.  A plug-in loaded into a host application
+// that owns all device memory may not allocate behind the host's back; a solver
+// running under a memory budget fixed at start-up may not grow; a real-time loop
+// sharing the GPU cannot afford cudaMalloc / cudaFree, which can synchronise the
+// whole device.  For them this entry point runs the same FP64 one-sided Jacobi as
+// the block-sparse SVD on one dense matrix, with all its working storage in a
+// file-scope device array instead of allocations.  The caller still passes the
+// input and output buffers.
 //
 // Scratch: g_svd_scratch below, QTT_SVD_NOALLOC_SCRATCH_BYTES (about 2.6 MB),
 // enough for m, n <= QTT_SVD_NOALLOC_MAX_DIM (256).  Every GPU that loads the
-// library holds it until the process exits.  All calls share it: two calls
-// whose work overlaps on the GPU (different streams, or different host threads
-// without ordering) race on it and corrupt each other's results.
+// library holds it until the process exits.  All calls share it and it keeps the
+// last call's contents: two calls whose work overlaps on the GPU (different
+// streams, or different host threads without ordering) race on it and corrupt
+// each other's results.  Every call writes every scratch element it reads.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address (cudaGetSymbolAddress) and the kernels' shared-memory
+// attributes for that device; make that first call before any stream capture.
+// The block width of the Jacobi kernel is never timed on this path, so a call
+// only issues work on the caller's stream and returns without waiting for it.
 #include <mutex>
 #include <string>
 
@@ -113,12 +121,14 @@ void svd_dense_noalloc(const double *a, int64_t m, int64_t n, double *u, double 
     k_na_pack<<<64, 256, 0, st>>>(a, int(m), int(n), W, d.trans);
     qtt::cuda_check(cudaGetLastError(), "no-alloc pack launch");
     // the Jacobi kernel initialises the rotation; the launcher clears the flags
-    qtt::launch_jacobi_on(st, W, rot, desc, slots, 1, std::max(1, qp - 1), kMaxSweeps, sweeps, flags, 0, d.p, d.q);
+    // tune = false: the block width is never timed here, so the call never waits on the stream
+    qtt::launch_jacobi_on(st, W, rot, desc, slots, 1, std::max(1, qp - 1), kMaxSweeps, sweeps, flags, 0, d.p, d.q,
+                          nullptr, 0, nullptr, nullptr, false);
     qtt::launch_finish_on(st, W, rot, Uc, Vc, s, desc, 1, d.q, scr, 0);
     k_na_rowmajor<<<64, 256, 0, st>>>(Uc, int(m), d.q, u);
     k_na_rowmajor<<<64, 256, 0, st>>>(Vc, int(n), d.q, v);
     qtt::cuda_check(cudaGetLastError(), "no-alloc layout launch");
-    qtt::count_launch(5);
+    qtt::count_launch(4);  // init, pack, two layout kernels (the Jacobi and finish launchers count theirs)
 }
 
 }  // namespace

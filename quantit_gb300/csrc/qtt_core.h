@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <functional>
 #include <cstdint>
 #include <cstring>
@@ -51,6 +52,38 @@ struct Error : std::exception {
 inline void cuda_check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) fail(e == cudaErrorMemoryAllocation ? ERR_OOM : ERR_CUDA,
                                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Kernel attributes (dynamic shared-memory limits) and device properties belong to
+// a device, so set-up done once per process would configure only the first device
+// a host thread used.  once_per_device runs f the first time it is reached with
+// a given device current (devices 0..63; a repeated f is harmless, so a race
+// between two threads costs at most one extra call).
+inline int current_device() {
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    return dev;
+}
+template <class F>
+void once_per_device(std::atomic<uint64_t> &done, F &&f) {
+    const int dev = current_device();
+    const uint64_t bit = (dev >= 0 && dev < 64) ? (uint64_t(1) << dev) : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return;
+    f();
+    if (bit) done.fetch_or(bit, std::memory_order_release);
+}
+// Streaming multiprocessors of the current device (cached per device).
+inline int device_sm_count() {
+    static std::atomic<int> cache[64];
+    const int dev = current_device();
+    if (dev >= 0 && dev < 64) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int nsm = 0;
+    cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    if (dev >= 0 && dev < 64) cache[dev].store(nsm, std::memory_order_relaxed);
+    return nsm;
 }
 
 // ---------------------------------------------------------------- charges

@@ -2,13 +2,14 @@
 mpotensor_*.txt of the reference, lines "l s s' r value" with 1-based indices,
 read as W[l-1, s-1, r-1, s'-1] by make_tensor in tests/2Dheisenberg.cpp:152-165)
 into tests/golden/heisenberg_cylinder_4x8_mpo.npz: one (l, s, r, s') dense
-array per site.  The physical basis of the fixture is {2Sz = -1, +1}."""
+array per site.  The physical basis of the fixture is {2Sz = -1, +1}.
+
+Usage: python make_cylinder_fixture.py <root of the QuantiT source tree>"""
 import os
 import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -26,11 +27,13 @@ def load(path):
     return w
 
 
-def main():
-    src = os.path.join(REF, "tests", "2dHeisenberg")
+def main(ref):
+    src = os.path.join(ref, "tests", "2dHeisenberg")
     ws = {f"w{i}": load(os.path.join(src, f"mpotensor_{i + 1}.txt")) for i in range(32)}
     np.savez_compressed(os.path.join(HERE, "heisenberg_cylinder_4x8_mpo.npz"), **ws)
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_cylinder_fixture.py <root of the QuantiT source tree>")
+    main(sys.argv[1])

@@ -1,11 +1,13 @@
 """The allocation-free dense SVD entry point (pytest -m gpu; collected last).
 
-qtt_svd_dense_noalloc serves callers that cannot allocate device memory (a
-captured graph region, a fixed memory budget, pre-registered buffers only): it
-works in a static device array instead.  Here it is called through the C-ABI
-with device buffers owned by the test, twice in a row, and compared with the
-library's regular SVD entry point (qtt_svd on a one-block btensor holding the
-same matrix) within the FP64 tolerances of the other SVD tests."""
+qtt_svd_dense_noalloc serves callers that cannot allocate device memory: a plug-in
+inside a host application that owns all device memory, a solver under a budget fixed
+at start-up, or a real-time loop that cannot afford cudaMalloc / cudaFree (they can
+synchronise the whole device).  It works in a static device array instead.  Here it
+is called through the C-ABI with device buffers owned by the test, twice in a row,
+and compared with the library's regular SVD entry point (qtt_svd on a one-block
+btensor holding the same matrix) and with LAPACK (numpy) within the FP64
+tolerances of the other SVD tests."""
 import ctypes as C
 
 import numpy as np
@@ -25,18 +27,21 @@ def _regular_svd(a):
     return U.block_at((0, 0)), d.block_at((0,)), V.block_at((0, 0))
 
 
-def _noalloc_svd(torch, a):
+def _noalloc_svd(torch, a, stream=None):
+    """One call on `stream` (a torch stream; default: the current one), read back
+    after that stream alone has been synchronised."""
     m, n = a.shape
     k = min(m, n)
     dev = torch.device("cuda", 0)
-    da = torch.as_tensor(a, dtype=torch.float64, device=dev).contiguous()
-    du = torch.full((m, k), np.nan, dtype=torch.float64, device=dev)
-    ds = torch.full((k,), np.nan, dtype=torch.float64, device=dev)
-    dv = torch.full((n, k), np.nan, dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    st = stream if stream is not None else torch.cuda.current_stream(dev)
+    with torch.cuda.stream(st):
+        da = torch.as_tensor(a, dtype=torch.float64, device=dev).contiguous()
+        du = torch.full((m, k), np.nan, dtype=torch.float64, device=dev)
+        ds = torch.full((k,), np.nan, dtype=torch.float64, device=dev)
+        dv = torch.full((n, k), np.nan, dtype=torch.float64, device=dev)
     _lib.call("qtt_svd_dense_noalloc", C.c_void_p(da.data_ptr()), m, n, C.c_void_p(du.data_ptr()),
-              C.c_void_p(ds.data_ptr()), C.c_void_p(dv.data_ptr()), C.c_void_p(stream.cuda_stream))
-    torch.cuda.synchronize(dev)
+              C.c_void_p(ds.data_ptr()), C.c_void_p(dv.data_ptr()), C.c_void_p(st.cuda_stream))
+    st.synchronize()
     return du.cpu().numpy(), ds.cpu().numpy(), dv.cpu().numpy()
 
 
@@ -53,13 +58,39 @@ def _check_same(a, got, want):
     np.testing.assert_allclose(v * sign, V, atol=1e-9)
 
 
+def _check_lapack(a, got):
+    """Independent reference: numpy's LAPACK SVD (values to 1e-12 of the largest;
+    factors orthonormal)."""
+    u, s, v = got
+    ref = np.linalg.svd(a, compute_uv=False)
+    np.testing.assert_allclose(s, ref, rtol=0, atol=1e-12 * ref[0])
+    k = s.size
+    np.testing.assert_allclose(u.T @ u, np.eye(k), atol=1e-12)
+    np.testing.assert_allclose(v.T @ v, np.eye(k), atol=1e-12)
+
+
 def test_noalloc_svd_matches_regular_entry_point_twice():
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(2024)
     shapes = [(120, 77), (64, 200)]
     for m, n in shapes:   # two calls in a row, the second reusing the scratch of the first
         a = rng.standard_normal((m, n)) * np.exp(-np.arange(n) / 20.0)
-        _check_same(a, _noalloc_svd(torch, a), _regular_svd(a))
+        got = _noalloc_svd(torch, a)
+        _check_same(a, got, _regular_svd(a))
+        _check_lapack(a, got)
+
+
+def test_noalloc_svd_on_a_non_default_stream():
+    """Two calls on a caller-created stream, each read after that stream's own
+    synchronisation."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    st = torch.cuda.Stream(device=torch.device("cuda", 0))
+    for m, n in [(256, 256), (31, 9)]:
+        a = rng.standard_normal((m, n))
+        got = _noalloc_svd(torch, a, stream=st)
+        _check_same(a, got, _regular_svd(a))
+        _check_lapack(a, got)
 
 
 def test_noalloc_svd_rejects_sizes_beyond_its_scratch():
