@@ -52,8 +52,8 @@ enum {
 enum { QTT_F64 = 0, QTT_F32 = 1 };
 /* precision of the block GEMMs (tensordot / matvec): FP64, or split TF32 (hi/lo) or
  * split BF16 (hi/mid/lo) on the tensor cores with FP32 accumulation.  Under a split
- * mode the sector SVD / eigh run in FP32; inner products, norms and the 2x2 solve
- * always run in FP64. */
+ * mode the sector SVD runs its first sweeps in FP32 and finishes them in FP64 (an FP64
+ * SVD either way); eigh, inner products, norms and the 2x2 solve always run in FP64. */
 enum { QTT_GEMM_F64 = 0, QTT_GEMM_TF32X3 = 1, QTT_GEMM_BF16X3 = 2 };
 
 /* ------------------------------------------------------------------ library */
@@ -75,11 +75,11 @@ int qtt_get_gemm_mode(void);
  * *len receives its length. */
 int qtt_set_autotune(int on);
 int qtt_autotune_report(char *buf, int64_t cap, int64_t *len);
-/* Deflation in the FP32 sector SVD of a truncating svd (split GEMM modes only; no
- * reference counterpart): off by default.  On: a column whose norm falls to FP32
- * epsilon x its sector's Frobenius norm or below leaves the sweeps, keeps that norm
- * as its singular value, and its left vector is an orthonormal completion of the
- * resolved ones (FP32 Householder).  Fewer sweeps, plus the cost of the completion. */
+/* Deflation in the sector SVD of a truncating svd (no reference counterpart; on by
+ * default): a column whose norm falls to the sweeps' resolution (FP32 epsilon, or 8
+ * FP64 epsilons, times its sector's Frobenius norm) leaves the sweeps and keeps that
+ * norm as its value, far below any value a truncation keeps; the FP64 sweeps of the
+ * mixed path resolve what its FP32 sweeps dropped. */
 int qtt_set_svd_deflation(int on);
 /* Persistent split-TF32 / split-BF16 GEMMs (one CTA per SM walking the tile list, double-buffered TMEM
  * accumulator) for launches of at least two tiles per SM; on by default (no reference
@@ -260,6 +260,9 @@ int64_t qtt_launch_count(void);
 /* Jacobi sweeps each sector needed in the most recent decomposition (synchronises);
  * *n receives the sector count, up to cap values are written to out. */
 int qtt_last_svd_sweeps(int32_t *out, int32_t cap, int32_t *n);
+/* Mixed path only: the FP32 sweeps each sector ran before its FP64 sweeps in the most
+ * recent decomposition (*n = 0 after a plain FP64 decomposition; synchronises). */
+int qtt_last_svd_fp32_sweeps(int32_t *out, int32_t cap, int32_t *n);
 
 #ifdef __cplusplus
 }

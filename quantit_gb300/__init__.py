@@ -26,8 +26,8 @@ def set_autotune(on):
 
 
 def set_svd_deflation(on):
-    """Deflate columns below FP32 resolution in the mixed path's truncating SVDs
-    (off by default)."""
+    """Under a truncating svd, numerically null columns (norm at the sweeps' FP32 / FP64
+    resolution) leave the sector-SVD sweeps (on by default)."""
     from ._lib import call
     call("qtt_set_svd_deflation", 1 if on else 0)
 

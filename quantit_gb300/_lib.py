@@ -85,6 +85,7 @@ SIGNATURES = {
     "qtt_stats_get": (C.c_int, [C.c_int, P(f64), P(f64), P(i64)]),
     "qtt_launch_count": (i64, []),
     "qtt_last_svd_sweeps": (C.c_int, [P(i32), i32, P(i32)]),
+    "qtt_last_svd_fp32_sweeps": (C.c_int, [P(i32), i32, P(i32)]),
     "qtt_svd_dense_noalloc": (C.c_int, [vp, i64, i64, vp, vp, vp, vp]),
 }
 

@@ -490,5 +490,12 @@ int qtt_last_svd_sweeps(int32_t *out, int32_t cap, int32_t *n) {
         for (int32_t i = 0; i < cap && i < int32_t(v.size()); ++i) out[i] = v[i];
     });
 }
+int qtt_last_svd_fp32_sweeps(int32_t *out, int32_t cap, int32_t *n) {
+    return guarded([&] {
+        auto v = qtt::last_svd_sweeps(true);
+        if (n) *n = int32_t(v.size());
+        for (int32_t i = 0; i < cap && i < int32_t(v.size()); ++i) out[i] = v[i];
+    });
+}
 
 }  // extern "C"

@@ -887,8 +887,7 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
             acc = fma(x, x, acc);
         }
         acc = wsum(acc);
-        // a deflated column keeps the norm it had when it left the sweeps (a value
-        // below FP32 resolution); its left vector is completed by k_complete_deflated
+        // a deflated column (dnorm given) keeps the norm it had when it left the sweeps
         const double dn = (dnorm && acc == 0.0) ? double(dnorm[sd.s_off + j]) : 0.0;
         if (lane == 0) {
             sig[j] = dn > 0.0 ? sqrt(dn) : sqrt(acc);
@@ -994,107 +993,6 @@ __global__ void __launch_bounds__(1024) k_finish(const T *__restrict__ work, con
     }
 }
 
-// Left vectors of the deflated columns of the SVD sectors (dpos 1, m of them, in
-// value order).  The resolved columns G (dpos 0, r of them, unit norm) are factored
-// by Householder QR in FP32, G = H_0 ... H_(r-1) R, and the j-th deflated column
-// becomes Q e_(r+j) = H_0 ... H_(r-1) e_(r+j): the completion vectors are orthonormal
-// and orthogonal to G to FP32 accuracy (r + m <= q <= p).  One CTA per sector;
-// scratch at coff[s] holds the p x r reflectors and one p-vector per warp.
-__global__ void __launch_bounds__(1024) k_complete_deflated(double *__restrict__ U, double *__restrict__ V,
-                                                            const SectorDesc *__restrict__ secs,
-                                                            const int *__restrict__ dpos, float *__restrict__ scratch,
-                                                            const int64_t *__restrict__ coff) {
-    extern __shared__ int csh[];  // good positions (q), deflated positions (q), tau (q floats)
-    __shared__ int s_r, s_m;
-    __shared__ float red[32];
-    __shared__ float s_scale;
-    const SectorDesc sd = secs[blockIdx.x];
-    if (sd.mode != 0) return;
-    const int p = sd.p, q = sd.q;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    int *gpos = csh;
-    int *dl = csh + q;
-    float *tau = reinterpret_cast<float *>(csh + 2 * q);
-    if (tid == 0) {
-        int r = 0, m = 0;
-        for (int j = 0; j < q; ++j) {
-            const int f = dpos[sd.s_off + j];
-            if (f == 0) gpos[r++] = j;
-            if (f == 1) dl[m++] = j;
-        }
-        s_r = r;
-        s_m = m;
-    }
-    __syncthreads();
-    const int r = s_r, m = s_m;
-    if (m == 0) return;
-    double *Wside = sd.trans ? (V + sd.v_off) : (U + sd.u_off);
-    float *A = scratch + coff[blockIdx.x];  // p x r, column-major
-    float *xs = A + int64_t(p) * r;         // nw vectors of length p
-    for (int64_t e = tid; e < int64_t(p) * r; e += blockDim.x) {
-        const int c = int(e / p), i = int(e - int64_t(c) * p);
-        A[e] = float(Wside[int64_t(gpos[c]) * p + i]);
-    }
-    __syncthreads();
-    for (int i = 0; i < r; ++i) {
-        float *a = A + int64_t(i) * p;
-        float part = 0.f;
-        for (int k = i + 1 + tid; k < p; k += blockDim.x) part = fmaf(a[k], a[k], part);
-        part = wsum(part);
-        if (lane == 0) red[warp] = part;
-        __syncthreads();
-        if (tid == 0) {
-            float xn2 = 0.f;
-            for (int k = 0; k < nw; ++k) xn2 += red[k];
-            const float alpha = a[i];
-            float t = 0.f, scale = 0.f;
-            if (xn2 > 0.f) {
-                const float beta = -copysignf(sqrtf(fmaf(alpha, alpha, xn2)), alpha);
-                t = (beta - alpha) / beta;
-                scale = 1.f / (alpha - beta);
-            }
-            tau[i] = t;
-            s_scale = scale;
-        }
-        __syncthreads();
-        const float scale = s_scale, ti = tau[i];
-        for (int k = i + 1 + tid; k < p; k += blockDim.x) a[k] *= scale;  // reflector (1, a[i+1:])
-        __syncthreads();
-        if (ti != 0.f) {
-            for (int c = i + 1 + warp; c < r; c += nw) {
-                float *b = A + int64_t(c) * p;
-                float d = 0.f;
-                for (int k = i + 1 + lane; k < p; k += 32) d = fmaf(a[k], b[k], d);
-                d = (wsum(d) + b[i]) * ti;
-                __syncwarp();
-                if (lane == 0) b[i] -= d;
-                for (int k = i + 1 + lane; k < p; k += 32) b[k] = fmaf(-d, a[k], b[k]);
-            }
-        }
-        __syncthreads();
-    }
-    float *x = xs + int64_t(warp) * p;
-    for (int j = warp; j < m; j += nw) {
-        const int col = r + j;
-        for (int k = lane; k < p; k += 32) x[k] = (k == col) ? 1.f : 0.f;
-        __syncwarp();
-        for (int i = r - 1; i >= 0; --i) {
-            const float ti = tau[i];
-            if (ti == 0.f) continue;
-            const float *a = A + int64_t(i) * p;
-            float d = 0.f;
-            for (int k = i + 1 + lane; k < p; k += 32) d = fmaf(a[k], x[k], d);
-            d = (wsum(d) + x[i]) * ti;
-            __syncwarp();
-            if (lane == 0) x[i] -= d;
-            for (int k = i + 1 + lane; k < p; k += 32) x[k] = fmaf(-d, a[k], x[k]);
-            __syncwarp();
-        }
-        double *dst = Wside + int64_t(dl[j]) * p;
-        for (int k = lane; k < p; k += 32) dst[k] = double(x[k]);
-        __syncwarp();
-    }
-}
 
 // Warm start: tmp = W V0 per sector in 64 x 64 tiles (256 threads, 4 x 4 outputs each,
 // K slabs of 16 through shared memory), then (mode 1) work <- tmp and rot <- V0.
@@ -1565,21 +1463,6 @@ void launch_warm_apply(void *work, void *rot, void *tmp, const WarmDesc *wd, int
     count_launch();
     count_launch();
     cuda_check(cudaGetLastError(), "warm-start kernel launch");
-}
-
-void launch_complete_deflated(double *U, double *V, const SectorDesc *sec, int nsec, const int *dpos, float *scratch,
-                              const int64_t *coff, int max_q) {
-    if (nsec <= 0) return;
-    const size_t smem = size_t(max_q) * 3 * sizeof(int);
-    if (smem > 200 * 1024) fail(ERR_INVALID_ARGUMENT, "sector too large for the completion kernel");
-    static std::atomic<uint64_t> attr{0};
-    once_per_device(attr, [] {
-        cuda_check(cudaFuncSetAttribute(k_complete_deflated, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                   "completion smem attribute");
-    });
-    k_complete_deflated<<<nsec, 1024, smem, ctx().stream>>>(U, V, sec, dpos, scratch, coff);
-    count_launch();
-    cuda_check(cudaGetLastError(), "completion kernel launch");
 }
 
 void launch_deflation_thresholds(const void *work, const SectorDesc *sec, int nsec, double delta, void *thr, int f32) {

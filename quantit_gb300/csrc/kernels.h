@@ -4,6 +4,7 @@
 #pragma once
 #include <atomic>
 #include <cstdint>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -198,6 +199,12 @@ struct WarmDesc {
     int32_t p, q, tile_start, pad;
 };
 void launch_warm_apply(void *work, void *rot, void *tmp, const WarmDesc *wd, int nwarm, int ntiles, int f32);
+// FP64 refinement of an FP32 sector decomposition (mixed path): from the FP32
+// rotations rot32 (at rot_off), vb <- the FP64-orthogonalised rotation (two
+// Newton-Schulz steps through va, with g as q x q scratch), w1 <- w64 vb (at w_off).
+// The FP64 Jacobi then runs warm on (w1, vb).
+void launch_svd_refine(const float *rot32, const double *w64, double *w1, double *va, double *vb, double *g,
+                       const std::vector<SectorDesc> &secs);
 // Segment = one input block (rows x cols at src_off) placed at rows [r0, r0+rows),
 // cols [c0, c0+cols) of sector `sector`.
 struct PackEntry {
@@ -230,12 +237,7 @@ void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot
 // thr[s] <- delta^2 ||W_s||_F^2 for every svd sector (0 for eigh), in the work type.
 void launch_deflation_thresholds(const void *work, const SectorDesc *sec, int nsec, double delta, void *thr, int f32);
 // dnorm (with defl; the work type, sum of q entries at s_off, zero on entry) receives
-// the squared norm of every deflated column; launch_finish keeps it as the column's
-// singular value and marks the column in dpos (s_off + output position: 0 resolved,
-// 1 deflated, 2 null), and launch_complete_deflated writes the deflated columns' left
-// vectors.  scratch: FP32, at coff[s] per sector p * (q + 32) elements.
-void launch_complete_deflated(double *U, double *V, const SectorDesc *sec, int nsec, const int *dpos, float *scratch,
-                              const int64_t *coff, int max_q);
+// the squared norm of every deflated column.
 size_t jacobi_vwork_bytes(int nsec, int64_t sum_q, int max_steps_per_sweep, int max_sweeps, int f32);
 // Column norms, sort (descending for svd, ascending eigenvalues for eigh),
 // normalisation and completion of null columns; writes U (m x k), V (n x k)

@@ -139,8 +139,10 @@ BT single_leg(const BT &like, const std::vector<int64_t> &sizes, const std::vect
 
 // sweep counts of the most recent decomposition (diagnostics)
 struct LastSweeps {
-    BufPtr buf;
+    BufPtr buf;       // sweeps of the stage that produced the factors
+    BufPtr pre;       // mixed path: sweeps of the FP32 stage
     int n = 0;
+    bool mixed = false;
 };
 LastSweeps &last_sweeps() {
     thread_local LastSweeps l;  // per host thread, like its stream
@@ -150,11 +152,8 @@ LastSweeps &last_sweeps() {
 // Set by svd_truncated around the decomposition it runs: its caller keeps only the
 // values the truncation selects, and the truncation never keeps a zero value
 // (btensor_linalg.cpp:658-755 keeps values strictly above the smallest kept one
-// less 2 eps, which is >= 0).  So null columns need no completion.  An FP32 sector
-// SVD there also deflates columns whose norm falls to FP32 epsilon x the sector's
-// Frobenius norm (below what FP32 arithmetic resolves): they leave the sweeps, keep
-// that last norm as their singular value, and get an orthonormal completion of the
-// resolved left vectors as theirs, so the factors stay isometries.
+// less 2 eps, which is >= 0).  So null columns need no completion, and numerically
+// null columns may leave the sweeps (deflation, below).
 struct TruncHint {
     bool active = false;
     int64_t min_size = 0;
@@ -173,6 +172,7 @@ struct ScopedTruncHint {
     ~ScopedTruncHint() { trunc_hint() = saved; }
 };
 constexpr double kDeflateF32 = 1.1920928955078125e-07;  // FP32 epsilon (2^-23)
+constexpr double kDeflateF64 = 8.0 * 2.220446049250313e-16;  // 8 x FP64 epsilon (2^-49)
 
 struct Decomp {
     std::vector<Sector> secs;
@@ -221,8 +221,10 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
     }
     D.total_k = stot;
     const int nsec = int(D.desc.size());
-    // the mixed path (split-precision block GEMMs) also runs its sector SVDs in FP32
-    const int f32 = gemm_mode() != GEMM_F64 ? 1 : 0;
+    // The mixed path (split-precision block GEMMs) runs its SVD sweeps in FP32 first and
+    // finishes them in FP64 (svd_refine.cu): the result is an FP64 SVD either way.  eigh
+    // always runs in FP64.
+    const int f32 = (mode == 0 && gemm_mode() != GEMM_F64) ? 1 : 0;
     const size_t es = f32 ? 4 : 8;
     D.work = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * es);
     D.rot = dev_alloc(size_t(std::max<int64_t>(rtot, 1)) * es);
@@ -293,88 +295,109 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
         }
     }
     SectorDesc *dsec = static_cast<SectorDesc *>(upload(D.desc.data(), D.desc.size() * sizeof(SectorDesc)));
+    const int64_t packed = std::accumulate(lens.begin(), lens.end(), int64_t(0));
+    const PackEntry *dpe = upload_vec(pe);
     auto chunks = make_chunks(lens);
+    const Chunk *dch = upload_vec(chunks);
     {
-        StatScope sc(ST_PACK, 2.0 * 8.0 * double(std::accumulate(lens.begin(), lens.end(), int64_t(0))));
-        launch_pack(static_cast<const double *>(t.data()), W, upload_vec(pe), upload_vec(chunks),
-                    int64_t(chunks.size()), dsec, f32);
+        StatScope sc(ST_PACK, 2.0 * 8.0 * double(packed));
+        launch_pack(static_cast<const double *>(t.data()), W, dpe, dch, int64_t(chunks.size()), dsec, f32);
     }
     if (mode == 1) launch_eigh_prepare(W, dsec, nsec, upper, f32);
     const int max_sweeps = 80;
     auto ibuf = dev_alloc(size_t(nsec) * (max_sweeps + 1) * sizeof(int));
     int *sweeps = static_cast<int *>(ibuf->p);
     int *flags = sweeps + nsec;
-    last_sweeps() = {ibuf, nsec};
     BufPtr scratch = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
-    if (stats_enabled()) {
-        // algorithmic work: every pair evaluation of every sweep (dots 6p, rotation 6p, V 6q),
-        // resolved from the sweep counts when the statistics are read (no sync here)
-        std::vector<std::pair<int, int>> pq;
-        for (auto &d : D.desc) pq.push_back({d.p, d.q});
-        BufPtr keep = ibuf;
-        stats_defer_work(ST_SVD, [keep, pq, nsec]() {
-            std::vector<int> sw(nsec);
-            cuda_check(cudaMemcpy(sw.data(), keep->p, size_t(nsec) * sizeof(int), cudaMemcpyDeviceToHost),
-                       "read sweeps");
-            double w = 0;
-            for (int s = 0; s < nsec; ++s)
-                w += double(sw[s]) * 0.5 * double(pq[s].second) * double(pq[s].second - 1) *
-                     (12.0 * pq[s].first + 6.0 * pq[s].second);
-            return w;
-        });
+    // algorithmic work of the decomposition: the LAPACK-class SVD count per p x q sector,
+    // 4 p^2 q + 8 p q^2 + 9 q^3 (eigh: 9 q^3), independent of the method
+    double algo = 0;
+    for (const SectorDesc &d : D.desc) {
+        const double P = d.p, Q = d.q;
+        algo += mode == 1 ? 9.0 * Q * Q * Q : 4.0 * P * P * Q + 8.0 * P * Q * Q + 9.0 * Q * Q * Q;
     }
     {
-        StatScope sc(ST_SVD, 0.0);
+        StatScope sc(ST_SVD, algo);
         const size_t vb = jacobi_vwork_bytes(nsec, stot, max_steps, max_sweeps, f32);
         BufPtr vwork = dev_alloc(vb);
-        BufPtr thr, dnorm, dpos;
         // a truncation keeps only values above its (non-negative) threshold, never a
         // zero one: null columns need no completion under a truncating svd
         const int cap = (mode == 0 && trunc_hint().active) ? 0 : -1;
-        const bool deflate = mode == 0 && f32 && trunc_hint().active && svd_deflation();
-        if (deflate) {
-            thr = dev_alloc(size_t(nsec) * es);
-            dnorm = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * es);
-            dpos = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * sizeof(int));
-            cuda_check(cudaMemsetAsync(dnorm->p, 0, size_t(std::max<int64_t>(stot, 1)) * es, ctx().stream),
+        // Under a truncating svd, a column whose norm falls to the working precision's
+        // resolution (c eps ||W_s||_F) leaves the sweeps: numerically null columns would
+        // otherwise be rotated against each other for many sweeps to no effect.  Its
+        // last norm is kept as its value (below any threshold a truncation keeps).
+        const bool deflate = cap == 0 && svd_deflation();
+        auto deflation = [&](const void *w, int prec32, BufPtr &thr, BufPtr &dn) {
+            const size_t e = prec32 ? 4 : 8;
+            thr = dev_alloc(size_t(nsec) * e);
+            dn = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * e);
+            cuda_check(cudaMemsetAsync(dn->p, 0, size_t(std::max<int64_t>(stot, 1)) * e, ctx().stream),
                        "cudaMemsetAsync(dnorm)");
-            launch_deflation_thresholds(W, dsec, nsec, kDeflateF32, thr->p, f32);
-        }
+            launch_deflation_thresholds(w, dsec, nsec, prec32 ? kDeflateF32 : kDeflateF64, thr->p, prec32);
+        };
+        BufPtr thr, dnorm;
+        if (deflate) deflation(W, f32, thr, dnorm);
         if (!wdesc.empty()) {
             BufPtr tmp = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * es);
             launch_warm_apply(W, D.rot->p, tmp->p, upload_vec(wdesc), int(wdesc.size()), ntiles, f32);
         }
-        launch_jacobi(W, D.rot->p, dsec, upload_vec(slots), nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
+        const int *dslots = upload_vec(slots);
+        launch_jacobi(W, D.rot->p, dsec, dslots, nsec, max_steps, max_sweeps, sweeps, flags, f32, max_p, stot,
                       vwork->p, vb, deflate ? thr->p : nullptr, deflate ? dnorm->p : nullptr);
+        const void *fw = W, *fr = D.rot->p;
+        BufPtr w64, w1, va, vbuf, gbuf, ibuf64;
+        if (f32) {
+            // FP64 stage: the FP64 sector matrices, the FP32 rotations made orthogonal in
+            // FP64, W1 = W V, and FP64 Jacobi sweeps from that warm start
+            w64 = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
+            w1 = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
+            va = dev_alloc(size_t(std::max<int64_t>(rtot, 1)) * 8);
+            vbuf = dev_alloc(size_t(std::max<int64_t>(rtot, 1)) * 8);
+            gbuf = dev_alloc(size_t(std::max<int64_t>(rtot, 1)) * 8);
+            cuda_check(cudaMemsetAsync(w64->p, 0, size_t(wtot) * 8, ctx().stream), "cudaMemsetAsync(work64)");
+            launch_pack(static_cast<const double *>(t.data()), w64->p, dpe, dch, int64_t(chunks.size()), dsec, 0);
+            launch_svd_refine(static_cast<const float *>(D.rot->p), static_cast<const double *>(w64->p),
+                              static_cast<double *>(w1->p), static_cast<double *>(va->p),
+                              static_cast<double *>(vbuf->p), static_cast<double *>(gbuf->p), D.desc);
+            std::vector<SectorDesc> d64 = D.desc;
+            for (SectorDesc &d : d64) d.warm = 1;
+            const SectorDesc *dsec64 = upload_vec(d64);
+            ibuf64 = dev_alloc(size_t(nsec) * (max_sweeps + 1) * sizeof(int));
+            int *sw64 = static_cast<int *>(ibuf64->p);
+            const size_t vb64 = jacobi_vwork_bytes(nsec, stot, max_steps, max_sweeps, 0);
+            BufPtr vwork64 = dev_alloc(vb64);
+            dsec = const_cast<SectorDesc *>(dsec64);
+            BufPtr thr64;
+            dnorm.reset();
+            if (deflate) deflation(w1->p, 0, thr64, dnorm);
+            launch_jacobi(w1->p, vbuf->p, dsec64, dslots, nsec, max_steps, max_sweeps, sw64, sw64 + nsec, 0, max_p,
+                          stot, vwork64->p, vb64, deflate ? thr64->p : nullptr, deflate ? dnorm->p : nullptr);
+            fw = w1->p;
+            fr = vbuf->p;
+        }
+        last_sweeps() = {f32 ? ibuf64 : ibuf, ibuf, nsec, f32 != 0};
         BufPtr permbuf;
         int64_t max_elems = 0;
         if (cap == 0) {
             permbuf = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * sizeof(int));
             for (const SectorDesc &d : D.desc) max_elems = std::max(max_elems, int64_t(d.q) * (d.p + d.q));
         }
-        launch_finish(W, D.rot->p, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
-                      static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), f32, cap,
-                      deflate ? dnorm->p : nullptr, deflate ? static_cast<int *>(dpos->p) : nullptr,
-                      permbuf ? static_cast<int *>(permbuf->p) : nullptr, max_elems);
-        if (deflate) {
-            // left vectors of the deflated columns: an orthonormal completion (FP32 Householder)
-            std::vector<int64_t> coff(nsec);
-            int64_t ctot = 0;
-            for (int i = 0; i < nsec; ++i) {
-                coff[i] = ctot;
-                ctot += int64_t(D.desc[i].p) * (D.desc[i].q + 32);
-            }
-            BufPtr cs = dev_alloc(size_t(std::max<int64_t>(ctot, 1)) * sizeof(float));
-            launch_complete_deflated(static_cast<double *>(D.U->p), static_cast<double *>(D.V->p), dsec, nsec,
-                                     static_cast<const int *>(dpos->p), static_cast<float *>(cs->p), upload_vec(coff),
-                                     max_q);
-        }
+        launch_finish(fw, fr, static_cast<double *>(D.U->p), static_cast<double *>(D.V->p),
+                      static_cast<double *>(D.S->p), dsec, nsec, max_q, static_cast<double *>(scratch->p), 0, cap,
+                      dnorm ? dnorm->p : nullptr, nullptr, permbuf ? static_cast<int *>(permbuf->p) : nullptr,
+                      max_elems);
         if (ws) {
-            // this decomposition's rotations start the next one at the same bond
+            // this decomposition's rotations (of the first stage) start the next one at the same bond
             std::vector<WarmStart::Entry> next;
             for (int i = 0; i < nsec; ++i)
                 next.push_back(WarmStart::Entry{std::move(keys[i]), D.rot, D.desc[i].rot_off, f32});
             ws->entries = std::move(next);
+        }
+        if (f32) {
+            // keep the FP64 stage's buffers alive until the factors are scattered
+            D.work = w1;
+            D.rot = vbuf;
         }
     }
 }
@@ -510,11 +533,12 @@ SVDOut svd(const BT &t) {
 }
 
 // svd(A, split), btensor_linalg.cpp:503-534
-std::vector<int> last_svd_sweeps() {
+std::vector<int> last_svd_sweeps(bool first_stage) {
     LastSweeps &l = last_sweeps();
-    std::vector<int> out(l.n);
-    if (l.n && l.buf) {
-        cuda_check(cudaMemcpyAsync(out.data(), l.buf->p, size_t(l.n) * sizeof(int), cudaMemcpyDeviceToHost,
+    const BufPtr &src = first_stage ? (l.mixed ? l.pre : BufPtr()) : l.buf;
+    std::vector<int> out(src ? l.n : 0);
+    if (!out.empty()) {
+        cuda_check(cudaMemcpyAsync(out.data(), src->p, size_t(l.n) * sizeof(int), cudaMemcpyDeviceToHost,
                                    ctx().stream), "cudaMemcpyAsync(sweeps)");
         cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
     }
@@ -628,6 +652,12 @@ SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, dou
     }
     double smallest = sorted[last < 0 ? last + n : last];
     smallest -= 2.0 * smallest * 2.220446049250313e-16;
+    double dropped = 0.0, total = 0.0;
+    for (double v : sorted) {
+        const double w = std::pow(std::fabs(v), pw);
+        total += w;
+        if (!(v > smallest)) dropped += w;
+    }
     // walk the d blocks backwards
     BT &U = in.U;
     BT *V = has_v ? &in.V : nullptr;
@@ -681,6 +711,8 @@ SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, dou
     auto chunks = make_chunks(lens);
     launch_permute(d.data(), dd.data(), upload_vec(ents), upload_vec(chunks), int64_t(chunks.size()), 8);
     o.d = dd;
+    o.discarded = dropped;
+    o.total = total;
     return o;
 }
 

@@ -313,6 +313,9 @@ BT mul_lastleg(const BT &u, const BT &d);
 
 struct SVDOut {
     BT U, d, V;
+    // after a truncation: sum of |s|^pow over the dropped values and over all values
+    // (the discarded weight truncate_impl bounds by tol^pow, btensor_linalg.cpp:658-682)
+    double discarded = 0.0, total = 0.0;
 };
 SVDOut svd(const BT &t);                       // untruncated, rank >= 2, sectors on the last two legs
 SVDOut svd_split(const BT &t, int64_t split);  // svd(A, split)
@@ -339,7 +342,9 @@ struct EighOut {
 };
 EighOut eigh(const BT &t, bool upper);
 EighOut eigh_split(const BT &t, int64_t split);
-std::vector<int> last_svd_sweeps();  // Jacobi sweeps per sector of the last decomposition
+// Jacobi sweeps per sector of the last decomposition: of the FP64 sweeps that gave the
+// factors, or (first_stage) of the mixed path's FP32 sweeps before them (empty otherwise)
+std::vector<int> last_svd_sweeps(bool first_stage = false);
 
 // ---------------------------------------------------------------- precision of block GEMMs
 enum GemmMode : int {

@@ -204,7 +204,7 @@ void set_jacobi_variant(int v) {
 }
 int jacobi_variant() { return g_jacobi_variant; }
 namespace {
-std::atomic<int> g_svd_deflation{0};
+std::atomic<int> g_svd_deflation{1};
 std::atomic<int> g_persistent_gemm{1};
 }
 void set_persistent_gemm(int on) { g_persistent_gemm = on ? 1 : 0; }

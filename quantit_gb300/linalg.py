@@ -43,11 +43,14 @@ def eigh(tensor, split=None, upper=False):
     return btensor._wrap(d), btensor._wrap(U)
 
 
-def last_svd_sweeps():
+def last_svd_sweeps(fp32_stage=False):
     """Jacobi sweeps each sector needed in the calling thread's most recent
-    decomposition (no reference counterpart; synchronises)."""
+    decomposition: the FP64 sweeps that produced the factors, or with fp32_stage
+    the FP32 sweeps the mixed path ran before them (empty after a plain FP64
+    decomposition).  No reference counterpart; synchronises."""
+    name = "qtt_last_svd_fp32_sweeps" if fp32_stage else "qtt_last_svd_sweeps"
     n = C.c_int32()
-    _lib.call("qtt_last_svd_sweeps", None, 0, C.byref(n))
+    _lib.call(name, None, 0, C.byref(n))
     buf = (C.c_int32 * max(n.value, 1))()
-    _lib.call("qtt_last_svd_sweeps", buf, n.value, C.byref(n))
+    _lib.call(name, buf, n.value, C.byref(n))
     return list(buf[:n.value])

@@ -6,7 +6,9 @@ memory, one CTA per block pair and grid step) is the default; the scalar kernel
 for shared memory.  Both must give the same decomposition as numpy's SVD for
 sector shapes that exercise ragged last blocks, odd block counts (a phantom
 block in the round-robin), sectors narrower than one block, wide sectors
-(decomposed as A^T), graded and rank-deficient spectra."""
+(decomposed as A^T), graded and rank-deficient spectra.  The mixed path (FP32
+sweeps, then FP64 sweeps from the FP32 rotation made orthogonal in FP64) is held
+to the same FP64 tolerances."""
 import numpy as np
 import pytest
 
@@ -54,9 +56,9 @@ def _svd_with(t, kernel, mode):
 
 def _check(t, blocks, out, mode):
     U, d, V = out
-    # FP64 work: LAPACK agreement to 1e-12 of the sector's largest singular value;
-    # FP32 work (the mixed path): to a few FP32 ulps of it
-    rtol = 1e-12 if mode == "f64" else 3e-6
+    # LAPACK agreement to 1e-12 of the sector's largest singular value, for the plain
+    # FP64 path and the mixed path (whose FP32 sweeps are finished in FP64) alike
+    rtol = 1e-12
     dv = dict(d.blocks())
     new_section = {k[0]: k[1] for k, _ in U.blocks()}  # sector (row section) -> section of the new leg
     for i, (_, a) in enumerate(blocks):
@@ -68,7 +70,7 @@ def _check(t, blocks, out, mode):
     for k, a in blocks:
         np.testing.assert_allclose(got[k], a, atol=10 * rtol * float(np.max(np.abs(a))), rtol=0, err_msg=str(a.shape))
     nd = sum(d.section_sizes)
-    iso = 1e-11 if mode == "f64" else 1e-4
+    iso = 1e-11
     assert q.dot_all(U, U) == pytest.approx(nd, rel=iso)
     assert q.dot_all(V, V) == pytest.approx(nd, rel=iso)
 
@@ -148,68 +150,49 @@ def _isometry_error(F):
     return err
 
 
-@pytest.fixture
-def deflation():
-    q.set_svd_deflation(True)
-    yield
-    q.set_svd_deflation(False)
-
-
+@pytest.mark.parametrize("defl", [False, True])
 @pytest.mark.parametrize("kernel", ["block", "scalar"])
-def test_truncated_fp32_svd_deflates_unresolved_columns(kernel, deflation):
-    """svd with a cutoff on the mixed path with deflation on: columns whose norm falls
-    below FP32 epsilon x their sector's Frobenius norm leave the sweeps (never more
-    sweeps than without deflation).  The resolved values match LAPACK to FP32
-    accuracy, the rest stay below FP32 resolution, and the kept factors are
-    isometries."""
+def test_mixed_truncated_svd_is_fp64_accurate(kernel, defl):
+    """svd with a cutoff on the mixed path: FP32 sweeps, then FP64 sweeps from the
+    FP32 rotation made orthogonal in FP64.  All values, including those far below
+    FP32 resolution, match LAPACK to 1e-12 of their sector's largest; the kept
+    factors are isometries to FP64 precision; the FP64 stage needs fewer sweeps than
+    a plain FP64 decomposition from the identity.  With deflation on, numerically null
+    columns leave the sweeps and the FP64 sweeps still resolve everything else."""
     rng = np.random.default_rng(81)
     shapes, ranks = [(150, 130), (90, 80), (40, 40), (12, 9)], [30, 20, 10, 9]
     t, blocks = _low_rank_tensor(rng, shapes, ranks)
     q.set_autotune(False)
     q.set_jacobi_kernel(kernel)
-    q.set_gemm_mode("tf32x3")
+    q.set_svd_deflation(defl)
     try:
-        q.linalg.svd(t)
-        full_sweeps = _last_sweeps()
+        q.linalg.svd(t, 1, 1e-14, min_size=1, max_size=10 ** 6)
+        plain_sweeps = _last_sweeps()
+        assert q.linalg.last_svd_sweeps(fp32_stage=True) == []
+        q.set_gemm_mode("tf32x3")
         U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=1, max_size=10 ** 6)
-        defl_sweeps = _last_sweeps()
+        fp64_sweeps = _last_sweeps()
+        fp32_sweeps = q.linalg.last_svd_sweeps(fp32_stage=True)
     finally:
         q.set_jacobi_kernel("block")
         q.set_gemm_mode("f64")
+        q.set_svd_deflation(True)   # the default
         q.set_autotune(True)
-    assert max(defl_sweeps) <= max(full_sweeps), (defl_sweeps, full_sweeps)
+    assert len(fp32_sweeps) == len(fp64_sweeps) == len(blocks)
+    if not defl:
+        assert max(fp64_sweeps) < max(plain_sweeps), (fp64_sweeps, plain_sweeps)
     new_section = {k[0]: k[1] for k, _ in U.blocks()}
     dv = dict(d.blocks())
-    for i, ((_, a), r) in enumerate(zip(blocks, ranks)):
+    for i, (_, a) in enumerate(blocks):
         want = np.linalg.svd(a, compute_uv=False)
         got = dv[(new_section[i],)]
-        assert len(got) >= r
-        np.testing.assert_allclose(got[:r], want[:r], atol=4 * 3e-6 * want[0], rtol=0)
-        assert np.all(got[r:] < 1e-6 * want[0])  # unresolved values that did not deflate
-    assert _isometry_error(U) < 1e-5
-    assert _isometry_error(V) < 1e-5
+        assert len(got) >= int(np.sum(want > 1e-12 * want[0]))
+        np.testing.assert_allclose(got, want[:len(got)], atol=1e-12 * want[0], rtol=0)
+    assert _isometry_error(U) < 1e-11
+    assert _isometry_error(V) < 1e-11
     R = dict(U.mul(d).tensordot(V.conj(), ([1], [1])).blocks())
     for k, a in blocks:
-        np.testing.assert_allclose(R[k], a, atol=1e-5 * float(np.max(np.abs(a))), rtol=0)
-
-
-def test_truncated_fp32_svd_completes_deflated_left_vectors(deflation):
-    """Deflated columns keep their last norm as singular value (noise below FP32
-    resolution, kept by a small cutoff like the unresolved values of an undeflated
-    FP32 sweep) and get completed left vectors: U stays an isometry."""
-    rng = np.random.default_rng(82)
-    t, blocks = _low_rank_tensor(rng, [(30, 24), (50, 41)], [2, 5])
-    q.set_gemm_mode("tf32x3")
-    try:
-        U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=6, max_size=10 ** 6)
-    finally:
-        q.set_gemm_mode("f64")
-    assert sum(d.section_sizes) >= 7
-    assert _isometry_error(U) < 1e-5
-    assert _isometry_error(V) < 1e-5
-    R = dict(U.mul(d).tensordot(V.conj(), ([1], [1])).blocks())
-    for k, a in blocks:
-        np.testing.assert_allclose(R[k], a, atol=1e-5 * float(np.max(np.abs(a))), rtol=0)
+        np.testing.assert_allclose(R[k], a, atol=1e-12 * float(np.max(np.abs(a))), rtol=0)
 
 
 def test_truncated_svd_drops_exact_zero_values_like_the_oracle():
@@ -232,6 +215,6 @@ def test_truncated_svd_drops_exact_zero_values_like_the_oracle():
             U, d, V = q.linalg.svd(t, 1, 1e-10, min_size=20, max_size=10 ** 6)
         finally:
             q.set_gemm_mode("f64")
-            q.set_svd_deflation(False)
+            q.set_svd_deflation(True)   # the default
         assert sum(d.section_sizes) == sum(len(v) for _, v in do.blocks) == 10, mode
-        assert _isometry_error(U) < (1e-11 if mode == "f64" else 1e-5)
+        assert _isometry_error(U) < 1e-11

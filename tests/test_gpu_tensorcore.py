@@ -81,7 +81,7 @@ def test_tc_gemm_tensorgdot_epilogue(tc_mode):
 
 
 def test_mixed_dmrg_energy_close_to_fp64():
-    """Converged runs: the mixed paths (split-TF32 or split-BF16 block GEMMs, FP32 sector SVD)
+    """Converged runs: the mixed paths (split-TF32 or split-BF16 block GEMMs, FP64-finished sector SVD)
     reports the FP64 variational energy of its final state, which matches the
     plain FP64 path to better than 1e-8 per site.  (Its per-bond Ritz values carry
     ~1e-6 relative noise from FP32 accumulation and are not used for the result.)"""

@@ -240,7 +240,7 @@ def test_tuning_switches_and_dmrg_options_round_trip():
         q.set_persistent_gemm(on)
         q.set_svd_deflation(on)
         q.set_autotune(on)
-    q.set_svd_deflation(False)
+    q.set_svd_deflation(True)   # the default
     for kernel in ("scalar", "block"):
         q.set_jacobi_kernel(kernel)
     with pytest.raises(ValueError):
