@@ -202,6 +202,22 @@ void qtt_dmrg_options_default(qtt_dmrg_options *opt);
  * number, the sweep's last energy, the sweep's wall time in seconds. */
 typedef void (*qtt_dmrg_log_fn)(void *user, int64_t sweep, double energy, double seconds);
 
+/* dmrg_logger (include/dmrg_logger.h:27-99): init before the first sweep,
+ * it_log_all after every sweep (sweep number, energy, the sweep's wall seconds,
+ * its largest relative discarded weight -- sum of dropped s^2 over sum of all s^2 of
+ * a bond's truncation, the weight truncate_impl bounds, btensor_linalg.cpp:658-682 --
+ * and the current state), end_log_all once when the driver stops (the last sweep's
+ * number, the returned energy, the final state).  The state's handles belong to the
+ * library and live for the call only (qtt_bt_clone keeps one).  Any member may be
+ * NULL. */
+typedef struct {
+    void *user;
+    void (*init)(void *user, const qtt_dmrg_options *opt);
+    void (*it_log_all)(void *user, int64_t step, double energy, double seconds, double truncated_weight, int32_t L,
+                       const qtt_bt *mps, int64_t oc);
+    void (*end_log_all)(void *user, int64_t step, double energy, int32_t L, const qtt_bt *mps, int64_t oc);
+} qtt_dmrg_logger;
+
 /* details::compute_2sitesHamil for one pair (dmrg.h:66; dmrg.cpp:504-515) */
 int qtt_compute_2sites_hamil(qtt_bt w_left, qtt_bt w_right, qtt_bt *out);
 /* details::hamil2site_times_state (dmrg.h:64; dmrg.cpp:521-531) */
@@ -211,6 +227,10 @@ int qtt_one_step_lanczos(qtt_bt state, qtt_bt hamil, qtt_bt Lenv, qtt_bt Renv, q
                          double *a1, double *b);
 /* details::eig2x2Mat (dmrg.h:61; dmrg.cpp:544-572) */
 int qtt_eig2x2(double a0, double a1, double b, double *E, double *o, double *n);
+/* The all-ones edge environment over leg state_leg of a site tensor and leg mpo_leg of
+ * an MPO tensor (generate_env_impl, dmrg.cpp:371-391; edge_shape_prep :335-345): leg 0
+ * of the first sites for the left edge, leg 2 of the last sites for the right edge. */
+int qtt_trivial_edge(qtt_bt state, int32_t state_leg, qtt_bt mpo, int32_t mpo_leg, qtt_bt *out);
 /* compute_left_env / compute_right_env (dmrg.cpp:425-493) */
 int qtt_compute_left_env(qtt_bt W, qtt_bt A, qtt_bt Lenv, qtt_bt *out);
 int qtt_compute_right_env(qtt_bt W, qtt_bt A, qtt_bt Renv, qtt_bt *out);
@@ -220,6 +240,10 @@ int qtt_compute_right_env(qtt_bt W, qtt_bt A, qtt_bt Renv, qtt_bt *out);
  * *oc is the orthogonality centre in and out; *E0 the final energy. */
 int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
              qtt_dmrg_log_fn log_fn, void *log_user, double *E0);
+/* The same driver with the full logger interface (dmrg(bMPO&, bMPS&, const
+ * dmrg_options&, dmrg_logger&), dmrg.h:39): logger may be NULL. */
+int qtt_dmrg_logged(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
+                    const qtt_dmrg_logger *logger, double *E0);
 
 /* <psi|H|psi> and <psi|psi> of an MPS against an MPO, contracted in FP64
  * (contract(bMPS, bMPS, bMPO) and contract(bMPS, bMPS), include/MPT.h; sources/MPT.cpp:211-290). */

@@ -712,6 +712,10 @@ def truncate(U: BTensor, d: BTensor, V: Optional[BTensor], max_size: int, min_si
     li = compute_last_index(vd, tol, pw, min_size, max_size)
     smallest = vd[li] if vd.size else 0.0
     smallest = smallest - 2 * smallest * eps
+    # the discarded weight the threshold bounds (sum of dropped |s|^pow), relative to
+    # the total: reported by the GPU driver's logger, kept here as an attribute
+    allw = np.abs(vd) ** pw
+    dropped_rel = float(np.sum(allw[~(vd > smallest)]) / np.sum(allw)) if vd.size and np.sum(allw) > 0 else 0.0
     unitaries = [x for x in (U, V) if x is not None]
     pos = len(d.blocks)
     while pos > 0:
@@ -731,6 +735,7 @@ def truncate(U: BTensor, d: BTensor, V: Optional[BTensor], max_size: int, min_si
             for un in unitaries:
                 un.ssz[len(un.ssz) - (len(d.ssz) - sector)] = k
                 un.blocks[:] = [(ui, (ub[..., :k] if ui[-1] == sector else ub)) for ui, ub in un.blocks]
+    d.discarded_rel = dropped_rel
     return U, d, V
 
 
@@ -892,6 +897,7 @@ def dmrg_bond_update(mpo, h2, mps, env, oc, forward, opt: DmrgOptions):
     theta = tensordot(mps[oc], mps[oc + 1], [2], [0])
     E, theta = two_sites_update(theta, h2[oc], env[oc], env[oc + 3])
     u, d, v = svd_truncated(theta, 2, opt.cutoff, opt.minimum_bond, opt.maximum_bond)
+    opt.last_discarded = getattr(d, "discarded_rel", 0.0)
     nrm = math.sqrt(sum(float(np.sum(b ** 2)) for _, b in d.blocks))
     d = scale(d, 1.0 / nrm)
     if forward:
@@ -921,14 +927,18 @@ def dmrg(mpo: List[BTensor], mps: List[BTensor], oc: int, opt: DmrgOptions, log=
         init_pos -= 1
         oc -= 1
     energies = []
+    opt.truncated_weights = []
     for it in range(opt.maximum_iterations):
         E = None
+        worst = 0.0
         for _ in range(2 * n_step):
             E = dmrg_bond_update(mpo, h2, mps, env, oc, step == 1, opt)
+            worst = max(worst, opt.last_discarded)
             oc += step
             if oc == 0 or oc == L - 2:
                 step = -step
         energies.append(E)
+        opt.truncated_weights.append(worst)
         if log is not None:
             log(it, E, mps)
         prev, E0 = E0, E

@@ -87,6 +87,8 @@ SIGNATURES = {
     "qtt_last_svd_sweeps": (C.c_int, [P(i32), i32, P(i32)]),
     "qtt_last_svd_fp32_sweeps": (C.c_int, [P(i32), i32, P(i32)]),
     "qtt_svd_dense_noalloc": (C.c_int, [vp, i64, i64, vp, vp, vp, vp]),
+    "qtt_dmrg_logged": (C.c_int, [i32, P(vp), P(vp), P(i64), vp, vp, P(f64)]),
+    "qtt_trivial_edge": (C.c_int, [vp, i32, vp, i32, P(vp)]),
 }
 
 
@@ -97,6 +99,13 @@ class DmrgOptionsC(C.Structure):
 
 
 LOG_FN = C.CFUNCTYPE(None, vp, i64, f64, f64)
+LOG_INIT = C.CFUNCTYPE(None, vp, vp)
+LOG_IT = C.CFUNCTYPE(None, vp, i64, f64, f64, f64, i32, P(vp), i64)
+LOG_END = C.CFUNCTYPE(None, vp, i64, f64, i32, P(vp), i64)
+
+
+class DmrgLoggerC(C.Structure):
+    _fields_ = [("user", vp), ("init", LOG_INIT), ("it_log_all", LOG_IT), ("end_log_all", LOG_END)]
 
 _lib = None
 

@@ -432,8 +432,37 @@ int qtt_compute_right_env(qtt_bt W, qtt_bt A, qtt_bt R, qtt_bt *out) {
         *out = wrap(qtt::compute_right_env(T(W), T(A), T(R)));
     });
 }
-int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
-             qtt_dmrg_log_fn log_fn, void *log_user, double *E0) {
+namespace {
+qtt::DmrgOpts dmrg_opts(const qtt_dmrg_options *opt) {
+    qtt::DmrgOpts o;
+    if (opt) {
+        o.cutoff = opt->cutoff;
+        o.convergence_criterion = opt->convergence_criterion;
+        o.maximum_bond = opt->maximum_bond;
+        o.minimum_bond = opt->minimum_bond;
+        o.maximum_iterations = opt->maximum_iterations;
+        o.gemm_mode = opt->gemm_mode;
+        o.final_energy_fp64 = opt->final_energy_fp64;
+        o.lanczos_steps = opt->lanczos_steps > 0 ? opt->lanczos_steps : 1;
+        o.cuda_graphs = opt->cuda_graphs;
+        o.svd_warm_start = opt->svd_warm_start;
+    }
+    return o;
+}
+
+// The state handed to a logger callback: handles that live for the call only.
+struct BorrowedMps {
+    std::vector<qtt_bt> h;
+    explicit BorrowedMps(const std::vector<qtt::BT> &mps) {
+        for (const qtt::BT &t : mps) h.push_back(wrap(qtt::BT(t)));
+    }
+    ~BorrowedMps() {
+        for (qtt_bt x : h) qtt_bt_destroy(x);
+    }
+};
+
+int run_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
+             const qtt::DmrgHooks &hooks, double *E0) {
     return guarded([&] {
         out_check(oc);
         out_check(E0);
@@ -443,21 +472,65 @@ int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_d
             W[i] = T(mpo[i]);
             S[i] = T(mps[i]);
         }
-        qtt::DmrgOpts o;
-        if (opt) {
-            o.cutoff = opt->cutoff;
-            o.convergence_criterion = opt->convergence_criterion;
-            o.maximum_bond = opt->maximum_bond;
-            o.minimum_bond = opt->minimum_bond;
-            o.maximum_iterations = opt->maximum_iterations;
-            o.gemm_mode = opt->gemm_mode;
-            o.final_energy_fp64 = opt->final_energy_fp64;
-            o.lanczos_steps = opt->lanczos_steps > 0 ? opt->lanczos_steps : 1;
-            o.cuda_graphs = opt->cuda_graphs;
-            o.svd_warm_start = opt->svd_warm_start;
-        }
-        *E0 = qtt::dmrg(W, S, *oc, o, log_fn, log_user);
+        *E0 = qtt::dmrg(W, S, *oc, dmrg_opts(opt), hooks);
         for (int i = 0; i < L; ++i) mps[i] = wrap(std::move(S[i]));
+    });
+}
+
+struct SimpleLog {
+    qtt_dmrg_log_fn fn;
+    void *user;
+};
+struct FullLog {
+    const qtt_dmrg_logger *lg;
+};
+}  // namespace
+
+int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
+             qtt_dmrg_log_fn log_fn, void *log_user, double *E0) {
+    SimpleLog sl{log_fn, log_user};
+    qtt::DmrgHooks hk;
+    if (log_fn) {
+        hk.user = &sl;
+        hk.sweep = [](void *u, int64_t it, double E, double secs, double, const std::vector<qtt::BT> &, int64_t) {
+            auto *s = static_cast<SimpleLog *>(u);
+            s->fn(s->user, it, E, secs);
+        };
+    }
+    return run_dmrg(L, mpo, mps, oc, opt, hk, E0);
+}
+
+int qtt_dmrg_logged(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
+                    const qtt_dmrg_logger *logger, double *E0) {
+    FullLog fl{logger};
+    qtt::DmrgHooks hk;
+    if (logger) {
+        if (logger->init) logger->init(logger->user, opt);
+        hk.user = &fl;
+        hk.sweep = [](void *u, int64_t it, double E, double secs, double trunc, const std::vector<qtt::BT> &m,
+                      int64_t c) {
+            const qtt_dmrg_logger *lg = static_cast<FullLog *>(u)->lg;
+            if (!lg->it_log_all) return;
+            BorrowedMps b(m);
+            lg->it_log_all(lg->user, it, E, secs, trunc, int32_t(b.h.size()), b.h.data(), c);
+        };
+        hk.done = [](void *u, int64_t it, double E, const std::vector<qtt::BT> &m, int64_t c) {
+            const qtt_dmrg_logger *lg = static_cast<FullLog *>(u)->lg;
+            if (!lg->end_log_all) return;
+            BorrowedMps b(m);
+            lg->end_log_all(lg->user, it, E, int32_t(b.h.size()), b.h.data(), c);
+        };
+    }
+    return run_dmrg(L, mpo, mps, oc, opt, hk, E0);
+}
+
+int qtt_trivial_edge(qtt_bt state, int32_t state_leg, qtt_bt mpo, int32_t mpo_leg, qtt_bt *out) {
+    return guarded([&] {
+        out_check(out);
+        const qtt::BT &s = T(state), &w = T(mpo);
+        if (state_leg < 0 || state_leg >= s.rank || mpo_leg < 0 || mpo_leg >= w.rank)
+            qtt::fail(qtt::ERR_INVALID_ARGUMENT, "edge leg out of range");
+        *out = wrap(qtt::trivial_edge(s, state_leg, w, mpo_leg));
     });
 }
 

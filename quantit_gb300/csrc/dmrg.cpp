@@ -296,7 +296,6 @@ LanczosHost one_step_lanczos(const BT &state, const BT &hamil, const BT &L, cons
     return o;
 }
 
-namespace {
 BT trivial_edge(const BT &st, int sleg, const BT &w, int wleg) {
     // all-ones rank-3 edge (generate_env_impl, dmrg.cpp:371-391; edge_shape_prep :335-345)
     BT e;
@@ -340,7 +339,6 @@ BT trivial_edge(const BT &st, int sleg, const BT &w, int wleg) {
     }
     return e;
 }
-}  // namespace
 
 namespace {
 double sum_all(const BT &t) {
@@ -371,8 +369,8 @@ double mps_energy(const std::vector<BT> &mpo, const std::vector<BT> &mps, double
     return e;
 }
 
-double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, const DmrgOpts &opt, DmrgLog log,
-            void *user) {
+double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, const DmrgOpts &opt,
+            const DmrgHooks &hooks) {
     const int64_t L = int64_t(mpo.size());
     if (L < 2 || int64_t(mps.size()) != L) fail(ERR_INVALID_ARGUMENT, "MPO and MPS need the same length >= 2");
     ScopedGemmMode guard(opt.gemm_mode);
@@ -407,9 +405,11 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
         double *p;
         ~HostFree() { cudaFreeHost(p); }
     } hf{hscal};
-    for (int64_t it = 0; it < opt.maximum_iterations; ++it) {
+    int64_t it = 0;
+    for (; it < opt.maximum_iterations; ++it) {
         auto t0 = std::chrono::steady_clock::now();
         double E = 0.0;
+        double trunc = 0.0;  // the sweep's largest relative discarded weight
         for (int64_t k = 0; k < 2 * n_step; ++k) {
             const bool forward = step == 1;
             DevScratch scr;
@@ -432,6 +432,7 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
                                      warm.empty() ? nullptr : &warm[size_t(oc)]);  // syncs
             if (hscal[6] != 0.0) fail(ERR_LOGIC, "nan found in output tensor");
             E = hscal[3];
+            if (f.total > 0.0) trunc = std::max(trunc, f.discarded / f.total);
             // d /= sqrt(sum(d.pow(2)))  (dmrg.cpp:188)
             launch_normalize(static_cast<double *>(f.d.data()), f.d.nnz, nullptr);
             if (forward) {
@@ -457,11 +458,12 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
             const double e = mps_energy(mpo, mps, &n2);
             E = e / n2;
         }
-        if (log) log(user, it, E, secs);
+        if (hooks.sweep) hooks.sweep(hooks.user, it, E, secs, trunc, mps, oc);
         double prev = E0;
         E0 = E;
         if (!(std::fabs((E0 - prev) / E0) > opt.convergence_criterion)) break;
     }
+    // `it`: the sweep that met the criterion, or maximum_iterations (dmrg.cpp:238-270)
     if (oc != init_pos) {
         if (oc != init_pos - 1 && init_pos != L - 1)
             fail(ERR_RUNTIME, "the orthogonality center finished somewhere surprising! final oc: " +
@@ -475,6 +477,7 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
         const double e = mps_energy(mpo, mps, &n2);
         E0 = e / n2;
     }
+    if (hooks.done) hooks.done(hooks.user, it, E0, mps, oc_io);
     return E0;
 }
 

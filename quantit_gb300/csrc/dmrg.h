@@ -27,7 +27,16 @@ struct LanczosKOut {
     int dim = 0;  // Krylov dimension used (smaller than k after a breakdown)
 };
 LanczosKOut lanczos_k(const BT &state, const BT &hamil, const BT &L, const BT &R, int k, bool graphs = true);
-typedef void (*DmrgLog)(void *user, int64_t sweep, double energy, double seconds);
+// Sweep hooks of the driver (dmrg_logger, include/dmrg_logger.h:27-99): `sweep` after
+// every sweep (it_log_all) with the sweep's largest relative discarded weight
+// (sum of dropped s^2 / sum of all s^2 over its bonds' truncations), `done` once when
+// the driver stops (end_log_all).  mps is the current state, oc its centre.
+struct DmrgHooks {
+    void *user = nullptr;
+    void (*sweep)(void *user, int64_t it, double E, double seconds, double trunc, const std::vector<BT> &mps,
+                  int64_t oc) = nullptr;
+    void (*done)(void *user, int64_t it, double E, const std::vector<BT> &mps, int64_t oc) = nullptr;
+};
 
 struct LanczosOut {
     BT psi;
@@ -45,8 +54,11 @@ void eig2x2(double a0, double a1, double b, double &E, double &o, double &n);
 LanczosOut one_step_lanczos_dev(const BT &state, const BT &hamil, const BT &L, const BT &R, double *scal,
                                 DevScratch &scr);
 LanczosHost one_step_lanczos(const BT &state, const BT &hamil, const BT &L, const BT &R);
-double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc, const DmrgOpts &opt, DmrgLog log,
-            void *user);
+double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc, const DmrgOpts &opt,
+            const DmrgHooks &hooks = DmrgHooks());
+// the all-ones rank-3 edge environment over leg sleg of st and leg wleg of w
+// (generate_env_impl, dmrg.cpp:371-391; edge_shape_prep :335-345)
+BT trivial_edge(const BT &st, int sleg, const BT &w, int wleg);
 double mps_energy(const std::vector<BT> &mpo, const std::vector<BT> &mps, double *norm2);
 
 }  // namespace qtt
