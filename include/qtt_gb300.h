@@ -245,6 +245,14 @@ int qtt_dmrg(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_d
 int qtt_dmrg_logged(int32_t L, const qtt_bt *mpo, qtt_bt *mps, int64_t *oc, const qtt_dmrg_options *opt,
                     const qtt_dmrg_logger *logger, double *E0);
 
+/* random_bMPS(bond_dim, mpo, constraint, seed) (include/MPT.h:49-53, sources/MPT.cpp:424-462):
+ * out[L] receives new rank-3 site tensors whose physical legs are the MPO's leg 1, with
+ * total charge constraint[ncomp] (the MPO's group) and bond sectors capped to bond_dim.
+ * Entries are N(0, 1) from a counter-based generator keyed by (seed, site, element),
+ * each site scaled to unit Frobenius norm; the orthogonality centre is the last site. */
+int qtt_random_mps(int32_t L, const qtt_bt *mpo, int64_t bond_dim, const int16_t *constraint, uint64_t seed,
+                   qtt_bt *out);
+
 /* <psi|H|psi> and <psi|psi> of an MPS against an MPO, contracted in FP64
  * (contract(bMPS, bMPS, bMPO) and contract(bMPS, bMPS), include/MPT.h; sources/MPT.cpp:211-290). */
 int qtt_mps_energy(int32_t L, const qtt_bt *mpo, const qtt_bt *mps, double *energy, double *norm2);

@@ -1028,6 +1028,31 @@ def dense_mpo_to_block(ws: List[np.ndarray], phys_q: List[int]) -> List[BTensor]
     return out
 
 
+def coalesce(mpo: List[BTensor], cutoff: float = 0.0) -> List[BTensor]:
+    """bMPO::coalesce, sources/MPT.cpp:154-168: one left-to-right pass of truncating
+    SVDs over the right bond of each site, W_i (l, s, r, s') -> (l, s, s', r),
+    U d V^H = svd(W_i, 3, cutoff); W_i <- (U d) permuted back, W_(i+1) <- V^H W_(i+1)."""
+    out = list(mpo)
+    for i in range(len(out) - 1):
+        U, d, V = svd_truncated(permute(out[i], [0, 1, 3, 2]), 3, cutoff, 1, 2 ** 62)
+        out[i + 1] = tensordot(conj(V), out[i + 1], [0], [0])
+        out[i] = permute(mul_lastleg(U, d), [0, 1, 3, 2])
+    return out
+
+
+def mps_overlap(a: List[BTensor], b: List[BTensor]) -> float:
+    """contract(bMPS a, bMPS b), sources/MPT.cpp:267-290: a[i] and conj(b[i])
+    contracted left to right (real tensors; the edge legs have size one)."""
+    env = None
+    for x, y in zip(a, b):
+        if env is None:
+            env = tensordot(x, conj(y), [0, 1], [0, 1])            # (r_a, r_b)
+        else:
+            t = tensordot(env, x, [0], [0])                         # (r_b, s, r_a)
+            env = tensordot(t, conj(y), [0, 1], [0, 1])             # (r_a', r_b')
+    return sum(float(np.sum(v)) for _, v in env.blocks)
+
+
 def heisenberg_mpo(L: int, J: float = -1.0, delta: float = 1.0) -> List[BTensor]:
     """Spin-1/2 Heisenberg (XXZ when delta != 1) chain MPO with U(1) total-2Sz
     charges (physical sections (1, +1), (1, -1) as in tests/DMRG_heisenberg_test.h:25-26)."""
@@ -1145,3 +1170,45 @@ def mps_energy(mpo: List[BTensor], mps: List[BTensor]) -> float:
     for W, A in zip(mpo, mps):
         env = compute_left_env(W, A, env)
     return float(sum(np.sum(b) for _, b in env.blocks))
+
+
+# --------------------------------------------------------------------------
+# block-list files written by quantit_gb300.serialize (np.savez archives), read
+# into oracle tensors so the CPU checks and baselines run on the GPU path's states
+# --------------------------------------------------------------------------
+
+
+def from_arrays(d) -> BTensor:
+    """One tensor from its arrays: sbd, ssz, cv [nsec][ncomp], sel, mods, bidx
+    [nblocks][rank] (block-list order) and data (the blocks concatenated)."""
+    mods = tuple(int(m) for m in np.asarray(d["mods"]).reshape(-1))
+    nc = len(mods)
+
+    def charge(vals):
+        return tuple((int(v) & 0xFFFF) if m else int(v) for v, m in zip(vals, mods))
+    sbd = [int(x) for x in np.asarray(d["sbd"]).reshape(-1)]
+    ssz = [int(x) for x in np.asarray(d["ssz"]).reshape(-1)]
+    cv = [charge(row) for row in np.asarray(d["cv"]).reshape(-1, nc)] if ssz else []
+    t = BTensor(mods, sbd, ssz, cv, charge(np.asarray(d["sel"]).reshape(-1)), [], np.float64)
+    bidx = np.asarray(d["bidx"]).reshape(-1, max(len(sbd), 1)) if len(sbd) else np.zeros((0, 0), int)
+    data = np.asarray(d["data"], dtype=np.float64) if "data" in d else None
+    off = 0
+    for row in bidx:
+        idx = tuple(int(x) for x in row)
+        shp = t.block_shape(idx)
+        n = int(np.prod(shp)) if shp else 1
+        t.blocks.append((idx, None if data is None else data[off:off + n].reshape(shp).copy()))
+        off += n
+    return t
+
+
+def load_npz(path):
+    """(kind, tensors, oc) of a file written by quantit_gb300.serialize.save."""
+    with np.load(path, allow_pickle=False) as z:
+        kind, n, oc = str(z["kind"]), int(z["count"]), int(z["oc"])
+        out = []
+        for i in range(n):
+            pre = f"t{i}_"
+            out.append(from_arrays({k[len(pre):]: z[k] for k in z.files if k.startswith(pre)}))
+    return kind, out, oc
+

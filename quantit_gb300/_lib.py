@@ -89,6 +89,7 @@ SIGNATURES = {
     "qtt_svd_dense_noalloc": (C.c_int, [vp, i64, i64, vp, vp, vp, vp]),
     "qtt_dmrg_logged": (C.c_int, [i32, P(vp), P(vp), P(i64), vp, vp, P(f64)]),
     "qtt_trivial_edge": (C.c_int, [vp, i32, vp, i32, P(vp)]),
+    "qtt_random_mps": (C.c_int, [i32, P(vp), i64, P(C.c_int16), C.c_uint64, P(vp)]),
 }
 
 

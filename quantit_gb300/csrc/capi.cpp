@@ -534,6 +534,20 @@ int qtt_trivial_edge(qtt_bt state, int32_t state_leg, qtt_bt mpo, int32_t mpo_le
     });
 }
 
+int qtt_random_mps(int32_t L, const qtt_bt *mpo, int64_t bond_dim, const int16_t *constraint, uint64_t seed,
+                   qtt_bt *out) {
+    return guarded([&] {
+        out_check(out);
+        if (L < 1) qtt::fail(qtt::ERR_INVALID_ARGUMENT, "need at least 1 site");
+        std::vector<qtt::BT> W(L);
+        for (int i = 0; i < L; ++i) W[i] = T(mpo[i]);
+        qtt::Charge q;
+        for (int i = 0; i < W[0].g.n; ++i) q.v[i] = constraint ? constraint[i] : 0;
+        std::vector<qtt::BT> S = qtt::random_mps(W, bond_dim, q, seed);
+        for (int i = 0; i < L; ++i) out[i] = wrap(std::move(S[i]));
+    });
+}
+
 int qtt_mps_energy(int32_t L, const qtt_bt *mpo, const qtt_bt *mps, double *energy, double *norm2) {
     return guarded([&] {
         out_check(energy);

@@ -340,6 +340,9 @@ SVDOut svd_truncated(const BT &t, int64_t split, double tol, int64_t min_size, i
 struct EighOut {
     BT d, U;
 };
+// random_bMPS(bond_dim, mpo, constraint, seed) (sources/MPT.cpp:424-462): one rank-3
+// site tensor per MPO site, total charge `target`, N(0, 1) entries, unit-norm sites.
+std::vector<BT> random_mps(const std::vector<BT> &mpo, int64_t D, const Charge &target, uint64_t seed);
 EighOut eigh(const BT &t, bool upper);
 EighOut eigh_split(const BT &t, int64_t split);
 // Jacobi sweeps per sector of the last decomposition: of the FP64 sweeps that gave the
