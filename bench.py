@@ -1,22 +1,27 @@
-"""Benchmark: seconds per two-site DMRG sweep at bond dimension D (default 2048).
+"""Benchmark: seconds per two-site DMRG sweep at bond dimension D = 2048, mixed
+precision against the plain FP64 path, on the spin-1/2 Heisenberg model of a 6 x 12
+open cylinder (72 sites, snake order, U(1) total Sz = 0).
 
-Workload: open spin-1/2 Heisenberg chain (U(1) total-Sz = 0), two-site DMRG with
-QuantiT's one-step Lanczos update, SVD cutoff 1e-10, max bond D, started from a
-seeded random MPS already at bond dimension D (sector dims = charge
-multiplicities capped to D) brought to right-canonical form.  One step = one
-full sweep (2(L-2) bond updates).  Synthetic data: no dataset is involved.
-
-Arms:
-  (default)          our CUDA path through libqtt_gb300.so (qtt_dmrg); block GEMMs
-                     in --mode (tf32x3 = split TF32 on tcgen05 tensor cores with an
-                     FP32 sector SVD -- the mixed path; bf16x3 = the same with
-                     split-BF16 operands; f64 = the plain drop-in).
-                     With --compare-f64 the plain FP64 path runs the same number of
-                     sweeps from the same state; both final states are evaluated in
-                     FP64 (<psi|H|psi>/<psi|psi>) for |dE| per site.
-  --impl reference   the CPU oracle (numpy restatement of QuantiT's algorithm) on
-                     the host cores; each step is one mid-chain bond update at D,
-                     extrapolated to a sweep by the sweep's size-weighted bond count.
+Workload (default, --model cylinder): H = J sum_<ij> S_i.S_j on the cylinder of
+circumference 6 and length 12, as an MPO compressed to its Schmidt rank (bond
+dimension 20).  A seeded random_bMPS at D = 256 is brought to canonical form and
+swept with QuantiT's two-site update (one-step Lanczos, SVD cutoff 1e-10) along the
+ramp D = 256 -> 512 -> 1024 (--ramp-sweeps each), then --warmup sweeps at D.  From
+that state S0:
+  value      : --steps mixed sweeps in ONE dmrg call (split-TF32 tensor-core block
+               GEMMs, sector SVDs finished in FP64), CUDA events on the library stream.
+  vs_fp64    : --compare-sweeps plain-FP64 sweeps from S0, set against the same number
+               of the timed mixed sweeps: seconds per sweep of each (sweeps after the
+               first of a call, which also builds the environments), and |dE| per site
+               between the two states' FP64 energies, with their truncated weights.
+  e2e        : one sweep per step through the public API from host buffers (upload the
+               MPS, one dmrg call, read the optimised MPS and energy back).
+  cpu_baseline / --impl reference: QuantiT's bond update restated in numpy (the
+               oracle) on the host cores, on the same state S0: real bond updates at
+               bonds spread evenly over the chain (stratified sample), times 2(L-2)
+               bond updates per sweep.
+Synthetic data: no dataset is involved.  Other workloads: --model heisenberg|hubbard
+(chains), --workload contraction|svd|serving.
 
 Prints one JSON line (rank 0).  Multi-GPU (torchrun) runs independent replicas,
 one solve per GPU ("replicas only": a DMRG sweep is sequential).
@@ -44,15 +49,30 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--model", default="heisenberg", choices=["heisenberg", "hubbard", "cylinder"],
+    p.add_argument("--model", default="cylinder", choices=["heisenberg", "hubbard", "cylinder"],
                    help="heisenberg: spin-1/2 chain, U(1) (defaults L=32, D=2048); hubbard: Fermi-Hubbard "
-                        "U=8 at half filling, U(1)xU(1) (defaults L=64, D=1024); cylinder: spin-1/2 Heisenberg "
-                        "on a 12 x 6 open cylinder, snake order (72 sites, long-range MPO; default D=512, "
-                        "reached by a bond-dimension ramp)")
+                        "U=8 at half filling, U(1)xU(1) (defaults L=64, D=1024); cylinder (default): spin-1/2 "
+                        "Heisenberg on a 6 x 12 open cylinder, snake order (72 sites, MPO compressed to bond "
+                        "dimension 20; D=2048 reached by the ramp 256 -> 512 -> 1024)")
     p.add_argument("--L", type=int, default=None)
     p.add_argument("--D", type=int, default=None)
     p.add_argument("--mode", default="tf32x3", choices=["f64", "tf32x3", "bf16x3"])
     p.add_argument("--compare-f64", type=int, default=1, help="also time FP64 sweeps from the same state")
+    p.add_argument("--compare-sweeps", type=int, default=2,
+                   help="cylinder: FP64 sweeps from the timed state for vs_fp64")
+    p.add_argument("--ramp-sweeps", type=int, default=2, help="cylinder: sweeps at each ramp bond dimension")
+    p.add_argument("--e2e-steps", type=int, default=2, help="cylinder: sweeps timed through the public API")
+    p.add_argument("--cpu-bonds", type=int, default=6, help="cylinder: bonds of the stratified CPU sample")
+    p.add_argument("--cpu-steps", type=int, default=3, help="cylinder: CPU bond updates in our arm's cpu_baseline")
+    p.add_argument("--prepare-cpu-sample", default=None,
+                   help="internal: build the timed state on the GPU and write it with the environments of "
+                        "the sampled bonds to this directory, then exit")
+    p.add_argument("--cpu-sample", default=None,
+                   help="internal: time oracle bond updates on the state written to this directory")
+    p.add_argument("--cpu-threads", type=int, default=0, help="internal: BLAS threads of --cpu-sample (0: all)")
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--svd-deflation", type=int, default=None,
+                   help="1/0: numerically null columns leave the sector-SVD sweeps of a truncating svd")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving", "contraction", "svd"],
                    help="dmrg: the D=2048 sweep line (with a short serving section); serving: the full "
@@ -410,6 +430,7 @@ def svd_workload(q, args):
         kinds = {k: q.stats.get(k) for k in q.stats.KINDS}
         q.stats.enable(False)
         sweeps = q.linalg.last_svd_sweeps()
+        fp32_sweeps = q.linalg.last_svd_sweeps(fp32_stage=True)
     finally:
         q.set_gemm_mode("f64")
         q.set_autotune(True)
@@ -421,7 +442,8 @@ def svd_workload(q, args):
                                                         f"of a Heisenberg L={args.L} D={args.D} DMRG state",
                                             "sweeps_before": args.svd_sweeps, "mode": args.mode,
                                             "l2": "flushed between steps (256 MB write)"},
-            "jacobi_sweeps_per_sector": sweeps, "kept": int(sum(d.section_sizes)),
+            "jacobi_sweeps_per_sector": sweeps, "fp32_sweeps_per_sector": fp32_sweeps,
+            "kept": int(sum(d.section_sizes)),
             "roofline": roofline("svd", kinds["svd"], peaks(), args.mode, {}),
             "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()}}
 
@@ -476,7 +498,7 @@ def contraction_workload(q, args):
     return {"metric": "s per block-sparse contraction + sector-SVD truncation (theta pair at D)",
             "value": m["total_s"], "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": m["total_s"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": f"{args.mode}+f32svd", "data": "synthetic",
+            "dtype": f"{args.mode}+f64svd", "data": "synthetic",
             "config": {"workload": f"theta-pair contraction C[a,s,u,c] = A[a,s,t,b] B[b,t,u,c] + svd(C, 2) "
                                    f"truncated to {D}", "D": D, "charges": "U(1) -8..8, Gaussian sections sigma=3",
                        "l2": "flushed between steps (256 MB write)", "seed": 0},
@@ -489,21 +511,357 @@ def contraction_workload(q, args):
             "kernel_time_ms": {k: v["ms"] for k, v in m["kinds"].items()}}
 
 
+# --------------------------------------------------------------------------- cylinder
+CYL_LX, CYL_LY = 12, 6      # open length x periodic circumference
+RAMP = (256, 512, 1024)     # bond dimensions swept before D
+
+
+def cylinder_mpo(q):
+    return q.networks.cylinder_heisenberg(CYL_LX, CYL_LY, 1.0, "snake", compress=True)
+
+
+def sweeps_call(q, mpo, mps, n, mode, D, logger=None):
+    """ONE dmrg call of n sweeps from mps (QuantiT's update, cutoff 1e-10, max bond D),
+    timed with CUDA events on the library stream: (seconds, energy, final state)."""
+    import torch
+    stream = torch.cuda.ExternalStream(q.lib().qtt_get_stream())
+    opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4,
+                                     maximum_iterations=n, gemm=mode, final_energy_fp64=False)
+    cur = q.networks.bMPS(list(mps), mps.orthogonality_center)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    E = q.algorithms.dmrg(mpo, cur, opts, logger)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3, E, cur
+
+
+def state_log(q, keep_after=None):
+    """dmrg_log_sweeptime that also keeps the state after sweep `keep_after`."""
+    class StateLog(q.algorithms.dmrg_log_sweeptime):
+        def __init__(self):
+            super().__init__()
+            self.kept = None
+
+        def it_log_all(self, step, energy, mps):
+            super().it_log_all(step, energy, mps)
+            if keep_after is not None and step + 1 == keep_after:
+                self.kept = mps
+    return StateLog()
+
+
+def prepare_cylinder(q, args, seed):
+    """The timed state S0: a seeded random_bMPS at RAMP[0] (canonical at site 0), swept
+    along the ramp and args.warmup times at args.D in args.mode."""
+    from quantit_gb300.conserved import Z
+    mpo = cylinder_mpo(q)
+    mps = q.networks.random_bMPS(RAMP[0], mpo, Z(0), seed=seed)
+    mps.move_oc(0)
+    mps.normalize_center()
+    info = {"ramp": []}
+    for Dr in RAMP:
+        if Dr >= args.D:
+            break
+        t, E, mps = sweeps_call(q, mpo, mps, args.ramp_sweeps, args.mode, Dr)
+        info["ramp"].append({"D": Dr, "sweeps": args.ramp_sweeps, "s": round(t, 2), "ritz_E": E})
+    log = state_log(q)
+    t, E, mps = sweeps_call(q, mpo, mps, max(args.warmup, 1), args.mode, args.D, log)
+    info["warmup"] = {"sweeps": max(args.warmup, 1), "s": round(t, 2), "ritz_E": log.energies,
+                      "truncated_weight": log.truncated_weights, "middle_bond": log.bond_list}
+    if len(log.energies) >= 2:
+        info["warmup"]["last_rel_dE"] = abs(log.energies[-1] - log.energies[-2]) / abs(log.energies[-1])
+    return mpo, mps, info
+
+
+def sample_bonds(L, n):
+    """n bonds spread evenly over 0..L-2 (the strata of the CPU sample)."""
+    n = max(1, min(n, L - 1))
+    return sorted({int((j + 0.5) * (L - 1) / n) for j in range(n)})
+
+
+def write_cpu_sample(q, mpo, mps, outdir, nbonds, D):
+    """The state, the MPO and the environments of the sampled bonds, for the oracle."""
+    from quantit_gb300 import serialize
+    os.makedirs(outdir, exist_ok=True)
+    bonds = sample_bonds(len(mps), nbonds)
+    serialize.save(os.path.join(outdir, "mpo.npz"), mpo)
+    serialize.save(os.path.join(outdir, "state.npz"), mps)
+    envs = q.algorithms.environments(mpo, mps, bonds)
+    for b, (Le, Re) in envs.items():
+        serialize.save(os.path.join(outdir, f"env_{b}.npz"), q.networks.bMPO([Le, Re]))
+    with open(os.path.join(outdir, "bonds.json"), "w") as f:
+        json.dump({"bonds": bonds, "L": len(mps), "Dmax": int(D)}, f)
+    return bonds
+
+
+def cpu_sample(path, steps, threads):
+    """Oracle bond updates (dmrg_2sites_update: theta, one-step Lanczos, truncated sector
+    SVD, environment update; sources/dmrg.cpp:145-207) on the saved state, cycling over
+    the sampled bonds; returns the seconds of every update per bond."""
+    from oracle import qtt_oracle as o
+    meta = json.load(open(os.path.join(path, "bonds.json")))
+    _, mpo, _ = o.load_npz(os.path.join(path, "mpo.npz"))
+    _, mps0, _ = o.load_npz(os.path.join(path, "state.npz"))
+    L = len(mps0)
+    h2 = o.compute_2sites_hamil(mpo)
+    envs = {}
+    for b in meta["bonds"]:
+        _, pair, _ = o.load_npz(os.path.join(path, f"env_{b}.npz"))
+        envs[b] = pair
+    opt = o.DmrgOptions(cutoff=1e-10, maximum_bond=int(meta["Dmax"]), minimum_bond=4)
+    bonds = meta["bonds"]
+    times = {b: [] for b in bonds}
+    for k in range(steps):
+        b = bonds[k % len(bonds)]
+        mps = list(mps0)
+        env = [None] * (L + 2)
+        env[b], env[b + 3] = envs[b]
+        t0 = time.perf_counter()
+        o.dmrg_bond_update(mpo, h2, mps, env, b, True, opt)
+        times[b].append(time.perf_counter() - t0)
+    return {"bonds": bonds, "times": {str(b): v for b, v in times.items()}, "threads": threads, "L": L}
+
+
+def run_cpu_sample(path, steps, threads):
+    """cpu_sample in a child process with `threads` BLAS threads (0: the default, all cores)."""
+    env = dict(os.environ)
+    if threads:
+        for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+            env[k] = str(threads)
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-sample", path, "--cpu-steps",
+                        str(steps), "--cpu-threads", str(threads)], capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"CPU sample failed: {r.stderr.strip()[-400:]}")
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def sweep_estimate(sample):
+    """Seconds per sweep from a stratified bond sample: the mean over strata of each
+    stratum's mean update time, times the 2(L-2) updates of a sweep."""
+    per = [float(np.mean(v)) for v in sample["times"].values() if v]
+    return float(np.mean(per)) * 2 * (sample["L"] - 2), per
+
+
+def cpu_host():
+    model = "unknown"
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return {"cpu": model, "nproc": os.cpu_count()}
+
+
+def cylinder_config(args):
+    ramp = "->".join(str(d) for d in RAMP if d < args.D)
+    return {"workload": f"Heisenberg 6x12 open cylinder (snake order, 72 sites), two-site DMRG sweep at "
+                        f"D={args.D} after the ramp {ramp}->{args.D}, U(1) Sz=0",
+            "L": CYL_LX * CYL_LY, "D": args.D,
+            "model": "spin-1/2 Heisenberg J=1 on an open cylinder of length 12 and circumference 6 "
+                     "(periodic), snake-ordered MPO compressed to its Schmidt rank (bond dimension 20)",
+            "cutoff": 1e-10, "update": "one-step Lanczos (QuantiT two_sites_update)",
+            "start": f"random_bMPS(256, seed={args.seed}), {args.ramp_sweeps} sweeps per ramp stage, "
+                     f"{args.warmup} warm-up sweeps at D",
+            "l2": "working set (MPS + environments, GBs) far larger than L2 (129 MB)"}
+
+
+def reference_arm_cylinder(args, cfg):
+    """The oracle's bond updates on the same state the GPU arm times (prepared on the GPU
+    in a child process, outside the timed region), all host cores; each step is one bond
+    update at a sampled bond; value = the stratified sweep estimate."""
+    import shutil
+    import tempfile
+    d = tempfile.mkdtemp(prefix="qtt_cpu_sample_")
+    try:
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--prepare-cpu-sample", d, "--D", str(args.D),
+               "--warmup", str(args.warmup), "--ramp-sweeps", str(args.ramp_sweeps), "--cpu-bonds",
+               str(args.cpu_bonds), "--mode", args.mode, "--seed", str(args.seed)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            return {"impl": "reference", "unavailable": "state preparation failed: " + r.stderr.strip()[-300:]}
+        # warm-up updates first, then the timed ones, cycling over the strata
+        smp = run_cpu_sample(d, args.warmup + args.steps, 0)
+        nb = len(smp["bonds"])
+        flat = []
+        for k in range(args.warmup + args.steps):
+            b = str(smp["bonds"][k % nb])
+            flat.append((b, smp["times"][b][k // nb]))
+        timed = {b: [] for b in smp["times"]}
+        for b, t in flat[args.warmup:]:
+            timed[b].append(t)
+        est, per = sweep_estimate({"times": timed, "L": smp["L"]})
+        one = run_cpu_sample(d, min(nb, 2), 1)
+        est1, _ = sweep_estimate(one)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    host = cpu_host()
+    sample = (f"{args.steps} oracle bond updates on the same D={args.D} state, cycling over bonds "
+              f"{smp['bonds']} (stratified: mean per stratum x {2 * (smp['L'] - 2)} updates per sweep); "
+              f"{host['nproc']} threads, {host['cpu']}")
+    return {"metric": METRIC, "value": est, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean([t for _, t in flat[args.warmup:]])) * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": est, "unit": UNIT, "cores": host["nproc"], "kind": "port", "sample": sample,
+                             "one_thread": {"value": est1, "unit": UNIT, "cores": 1,
+                                            "sample": f"{len(one['bonds'])} bond updates at 1 BLAS thread "
+                                                      f"(bonds {one['bonds'][:2]})"}},
+            "per_stratum_s": per,
+            "e2e": {"value": est, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def e2e_cylinder(q, mpo, mps, args):
+    """args.e2e_steps sweeps, each through the public API from host buffers: the MPS is
+    uploaded, one dmrg call runs, the optimised MPS and the energy are read back."""
+    host = [(t.copy_structure(), t.blocks()) for t in mps]
+    oc = mps.orthogonality_center
+    opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=args.D, min_bond=4,
+                                     maximum_iterations=1, gemm=args.mode, final_energy_fp64=False)
+    ts, h2d, d2h, E = [], [], [], None
+    for _ in range(max(1, args.e2e_steps)):
+        h2d.append(sum(sum(v.nbytes for _, v in blks) for _, blks in host))
+        t0 = time.perf_counter()
+        dev = q.networks.bMPS([st.set_blocks(b) for st, b in host], oc)
+        E = q.algorithms.dmrg(mpo, dev, opts)
+        out = [t.blocks() for t in dev]
+        ts.append(time.perf_counter() - t0)
+        d2h.append(sum(sum(v.nbytes for _, v in blks) for blks in out) + 8)
+        host = [(t.copy_structure(), blks) for t, blks in zip(dev, out)]
+        oc = dev.orthogonality_center
+    return {"value": float(np.mean(ts)), "unit": UNIT, "steps": len(ts), "sweep_times_s": ts,
+            "h2d_bytes_per_step": int(np.mean(h2d)), "d2h_bytes_per_step": int(np.mean(d2h)), "E": E,
+            "note": "one sweep per step through the public API from host buffers (state upload, one dmrg call "
+                    "that also builds the environments, state and energy read back)"}
+
+
+def cylinder_main(args, rank, world, local):
+    import torch
+    import quantit_gb300 as q
+    from quantit_gb300 import replicas
+    cfg = cylinder_config(args)
+    cfg["parallelism"] = "replicas only" if world > 1 else "single GPU"
+    t_prep = time.perf_counter()
+    mpo, S0, info = prepare_cylinder(q, args, replicas.replica_seed(args.seed, rank))
+    info["prep_wall_s"] = round(time.perf_counter() - t_prep, 1)
+    # the timed region: args.steps mixed sweeps in one dmrg call
+    q.stats.reset()
+    q.stats.enable(True)
+    sampler = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = q.stats.launches()
+    log = state_log(q, keep_after=args.compare_sweeps)
+    sampler.start()
+    t_mix, _, S_mix = sweeps_call(q, mpo, S0, args.steps, args.mode, args.D, log)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = q.stats.launches() - launches0
+    kinds = {k: q.stats.get(k) for k in q.stats.KINDS}
+    q.stats.enable(False)
+    t_step = replicas.max_over_ranks([t_mix / args.steps])[0]
+    line = {"metric": METRIC, "value": t_step / world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": f"{args.mode}+f64svd+f64" if args.mode != "f64" else "f64",
+            "data": "synthetic", "config": dict(cfg, mode=args.mode), "gpu_launches": int(launches),
+            "clocks": clocks}
+    P = peaks()
+    pc = {}
+    dom = max(kinds, key=lambda k: kinds[k]["ms"])
+    line["roofline"] = roofline(dom, kinds[dom], P, args.mode, pc)
+    line["roofline_gemm"] = roofline("gemm", kinds["gemm"], P, args.mode, pc)
+    line["kernel_time_ms"] = {k: round(v["ms"], 1) for k, v in kinds.items()}
+    line["sweeps"] = {"times_s": [round(x, 3) for x in log.time_list], "middle_bond": log.bond_list,
+                      "truncated_weight": log.truncated_weights, "ritz_E": log.energies}
+    # the same state in FP64: compare_sweeps sweeps, against the first as many timed mixed sweeps
+    if args.mode != "f64" and args.compare_f64:
+        n = max(1, min(args.compare_sweeps, args.steps))
+        lf = state_log(q)
+        _, _, S64 = sweeps_call(q, mpo, S0, n, "f64", args.D, lf)
+        t64 = lf.time_list[1:] if len(lf.time_list) > 1 else lf.time_list
+        tm = log.time_list[1:] if len(log.time_list) > 1 else log.time_list
+        Sm = log.kept if log.kept is not None else S_mix
+        E64, _ = fp64_energy(q, mpo, S64)
+        Em, _ = fp64_energy(q, mpo, Sm)
+        line["vs_fp64"] = {
+            "fp64_s_per_sweep": float(np.mean(t64)), "mixed_s_per_sweep": float(np.mean(tm)),
+            "speedup_vs_fp64": float(np.mean(t64)) / float(np.mean(tm)),
+            "dE_per_site": abs(Em - E64) / (CYL_LX * CYL_LY), "E_fp64": E64, "E_mixed": Em, "sweeps": n,
+            "truncated_weight_fp64": lf.truncated_weights, "truncated_weight_mixed": log.truncated_weights[:n],
+            "note": "both from the timed state; per-sweep wall times of the sweeps after the first of each call; "
+                    "energies are FP64 <psi|H|psi>/<psi|psi> after the same number of sweeps"}
+    line["state"] = info
+    line["e2e"] = e2e_cylinder(q, mpo, S0, args)
+    if rank == 0 and not args.no_cpu_baseline:
+        import shutil
+        import tempfile
+        d = tempfile.mkdtemp(prefix="qtt_cpu_sample_")
+        try:
+            write_cpu_sample(q, mpo, S0, d, args.cpu_bonds, args.D)
+            smp = run_cpu_sample(d, args.cpu_steps, 0)
+            est, per = sweep_estimate(smp)
+            host = cpu_host()
+            line["cpu_baseline"] = {"value": est, "unit": UNIT, "cores": host["nproc"], "kind": "port",
+                                    "sample": f"{args.cpu_steps} oracle bond updates on the timed state at bonds "
+                                              f"{smp['bonds'][:args.cpu_steps]} (stratified estimate x "
+                                              f"{2 * (smp['L'] - 2)} updates per sweep), {host['cpu']}"}
+        except Exception as e:  # reported, never hidden
+            line["cpu_baseline"] = {"error": repr(e)}
+        finally:
+            shutil.rmtree(d, ignore_errors=True)
+    tune = q.autotune_report().splitlines()
+    line["autotune_classes"] = len(tune)
+    if rank == 0:
+        print("autotune:\n  " + "\n  ".join(tune), file=sys.stderr)
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.cpu_sample:
+        print(json.dumps(cpu_sample(args.cpu_sample, args.cpu_steps, args.cpu_threads)))
+        return
+    if args.prepare_cpu_sample:
+        import quantit_gb300 as q
+        q.ensure_init(0)
+        if args.D is None:
+            args.D = 2048
+        mpo, S0, _ = prepare_cylinder(q, args, args.seed)
+        write_cpu_sample(q, mpo, S0, args.prepare_cpu_sample, args.cpu_bonds, args.D)
+        return
     rank, world, local = dist_env()
     hub = args.model == "hubbard"
     cyl = args.model == "cylinder"
+    if cyl and args.workload in ("svd", "contraction"):
+        args.model, cyl = "heisenberg", False   # these workloads take a chain's theta or the theta pair
     if args.L is None:
         args.L = 72 if cyl else (64 if hub else 32)
     if args.D is None:
-        args.D = 512 if cyl else (1024 if hub else 2048)
-    if cyl:
-        cfg = {"workload": f"Heisenberg 12x6 open cylinder (snake order, 72 sites), two-site DMRG sweep at "
-                           f"D={args.D} after a ramp from D={max(64, args.D // 4)}, U(1) Sz=0",
-               "L": 72, "D": args.D, "model": "spin-1/2 Heisenberg J=1 on an open cylinder Lx=12 x Ly=6 "
-                                               "(periodic around Ly), long-range MPO w=35"}
-    elif hub:
+        args.D = 1024 if hub else 2048
+    if cyl and args.workload == "dmrg":
+        if args.impl == "reference":
+            if rank == 0:
+                cfg = dict(cylinder_config(args), parallelism="single GPU")
+                print(json.dumps(reference_arm_cylinder(args, cfg)))
+            return
+        import torch
+        torch.cuda.set_device(local)
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl")
+        import quantit_gb300 as q
+        q.ensure_init(local)
+        q.set_jacobi_kernel(args.jacobi)
+        if args.svd_deflation is not None:
+            q.set_svd_deflation(bool(args.svd_deflation))
+        cylinder_main(args, rank, world, local)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    if hub:
         cfg = {"workload": f"Fermi-Hubbard chain L={args.L}, U=8, half filling, two-site DMRG sweep at D={args.D}, "
                            "U(1)xU(1) (N, 2Sz)", "L": args.L, "D": args.D,
                "model": "Fermi-Hubbard open chain t=1 U=8 mu=0, N=L, Sz=0"}
@@ -516,9 +874,9 @@ def main():
            "parallelism": "replicas only" if world > 1 else "single GPU"})
     if args.impl == "reference":
         if rank == 0:
-            if hub or cyl:
+            if hub:
                 print(json.dumps({"impl": "reference", "unavailable": "the CPU sampler restates the Heisenberg "
-                                  "chain's bond update only; this model runs on the GPU paths"}))
+                                  "bond update only; this model runs on the GPU paths"}))
             else:
                 print(json.dumps(reference_arm(args, cfg)))
         return
@@ -531,6 +889,8 @@ def main():
     import quantit_gb300 as q
     q.ensure_init(local)
     q.set_jacobi_kernel(args.jacobi)
+    if args.svd_deflation is not None:
+        q.set_svd_deflation(bool(args.svd_deflation))
     if args.workload in ("contraction", "svd"):
         line = (contraction_workload if args.workload == "contraction" else svd_workload)(q, args)
         if rank == 0:
@@ -544,7 +904,7 @@ def main():
             print(json.dumps({"metric": "solves/s (XXZ ground states, Poisson arrivals) at p99 latency",
                               "value": sv["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": 1,
                               "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                              "dtype": f"{args.mode if args.mode != 'f64' else 'tf32x3'}+f32svd+f64",
+                              "dtype": f"{args.mode if args.mode != 'f64' else 'tf32x3'}+f64svd+f64",
                               "data": "synthetic",
                               "config": {"workload": "serving: Poisson stream of XXZ chain ground-state solves",
                                          "parallelism": "replicas only" if world > 1 else "single GPU"},
@@ -554,10 +914,6 @@ def main():
         return
     from quantit_gb300 import replicas
     mpo, mps0 = build_state(q, args.L, args.D, seed=replicas.replica_seed(0, rank), model=args.model)
-    if cyl:  # bond-dimension ramp (one sweep per stage) before the sweeps at D
-        for Dr in (max(64, args.D // 4), max(64, args.D // 2)):
-            if Dr < args.D:
-                _, _, mps0 = run_sweeps(q, mpo, mps0, 1, args.mode, Dr)
     _, _, mps1 = run_sweeps(q, mpo, mps0, args.warmup, args.mode, args.D)
     q.stats.reset()
     q.stats.enable(True)
@@ -597,7 +953,7 @@ def main():
     dom = max(kinds, key=lambda k: kinds[k]["ms"])
     line = {"metric": METRIC, "value": job_per_sweep, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f32svd+f64",
+            "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f64svd+f64",
             "data": "synthetic", "config": dict(cfg, mode=args.mode, jacobi=args.jacobi), "ritz_energies": Es,
             "energy_fp64": E_mixed, "energy_per_site": E_mixed / args.L, "fp64_energy_eval_s": t_eval,
             "sweep_times_s": ts, "wall_s": wall, "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()},
@@ -612,7 +968,7 @@ def main():
     line["autotune_classes"] = len(tune)
     if rank == 0:
         print("autotune:\n  " + "\n  ".join(tune), file=sys.stderr)
-    if rank == 0 and not args.no_cpu_baseline and (hub or cyl):
+    if rank == 0 and not args.no_cpu_baseline and hub:
         line["cpu_baseline"] = None  # the oracle sampler restates the Heisenberg bond update only
     elif rank == 0 and not args.no_cpu_baseline:
         try:
@@ -624,7 +980,7 @@ def main():
                                               f"x {s.factor:.1f} size-weighted bonds per sweep"}
         except Exception as e:  # reported, never hidden
             line["cpu_baseline"] = {"error": repr(e)}
-    if rank == 0 and args.serving_requests > 0 and not (hub or cyl):
+    if rank == 0 and args.serving_requests > 0 and not hub:
         try:
             line["serving"] = serving_section(q, args, full=False)
         except Exception as e:  # reported, never hidden
