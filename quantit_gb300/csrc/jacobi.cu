@@ -1192,13 +1192,14 @@ int r_class(int max_p) {
 }
 
 // Block widths the block kernel is built with for (element type, R): FP32 16 (R <= 32)
-// and 8 (R <= 64); FP64 8 (R <= 48) and 16 (R <= 8, beyond that 16 warps run out of
-// registers).  The first entry is the default.
+// and 8 (R <= 64); FP64 8 and 4 (R <= 48).  The first entry is the default.
 std::vector<int> block_widths(bool f32, int R) {
     if (R == 0) return {};
     if (f32) return R <= 32 ? std::vector<int>{16, 8} : std::vector<int>{8};
     if (R > 48) return {};
-    return R <= 8 ? std::vector<int>{8, 16} : std::vector<int>{8};
+    // FP64: two SMs' worth of block pairs per sector at width 4 against one at 8; the
+    // FP64 pipe (2 FMA per clock per SM) rather than the round latency bounds a wide sector
+    return std::vector<int>{8, 4};
 }
 
 // Block kernel for columns up to 2048 (FP32) / 1536 (FP64) elements, as many
@@ -1220,7 +1221,7 @@ bool bjacobi_dispatch(const BJacobiParams<T> &P, int max_steps_per_sweep, int ma
         QTT_BJ(8, 4) QTT_BJ(8, 8) QTT_BJ(8, 16) QTT_BJ(8, 24) QTT_BJ(8, 32) QTT_BJ(8, 48) QTT_BJ(8, 64)
     } else {
         QTT_BJ(8, 4) QTT_BJ(8, 8) QTT_BJ(8, 16) QTT_BJ(8, 24) QTT_BJ(8, 32) QTT_BJ(8, 48)
-        QTT_BJ(16, 4) QTT_BJ(16, 8)
+        QTT_BJ(4, 4) QTT_BJ(4, 8) QTT_BJ(4, 16) QTT_BJ(4, 24) QTT_BJ(4, 32) QTT_BJ(4, 48)
     }
 #undef QTT_BJ
     return false;
