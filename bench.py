@@ -400,6 +400,14 @@ def svd_workload(q, args):
     from quantit_gb300 import serialize
     if args.state_file:
         theta = serialize.load(args.state_file)
+    elif args.model == "cylinder":
+        # the mid-cylinder theta of the state the headline times
+        mpo, cur, _ = prepare_cylinder(q, args, args.seed)
+        c = len(cur) // 2
+        cur.move_oc(c)
+        theta = cur[c].tensordot(cur[c + 1], ([2], [0]))
+        if args.save_state:
+            serialize.save(args.save_state, theta)
     else:
         mpo, mps = build_state(q, args.L, args.D, seed=0)
         _, _, cur = run_sweeps(q, mpo, mps, args.svd_sweeps, "tf32x3", args.D)
@@ -438,8 +446,10 @@ def svd_workload(q, args):
     return {"metric": "s per truncated sector SVD of a mid-chain DMRG theta", "value": t, "unit": "s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.mode != "f64" else "f64",
-            "data": "synthetic", "config": {"workload": f"svd(theta, 2, 1e-10, 1, {args.D}) of the mid-chain theta "
-                                                        f"of a Heisenberg L={args.L} D={args.D} DMRG state",
+            "data": "synthetic", "config": {"workload": f"svd(theta, 2, 1e-10, 1, {args.D}) of the middle theta "
+                                                        f"of a D={args.D} DMRG state of the "
+                                                        + ("6x12 cylinder" if args.model == "cylinder"
+                                                           else f"Heisenberg chain L={args.L}"),
                                             "sweeps_before": args.svd_sweeps, "mode": args.mode,
                                             "l2": "flushed between steps (256 MB write)"},
             "jacobi_sweeps_per_sector": sweeps, "fp32_sweeps_per_sector": fp32_sweeps,
@@ -770,7 +780,7 @@ def cylinder_main(args, rank, world, local):
             "clocks": clocks}
     P = peaks()
     pc = {}
-    dom = max(kinds, key=lambda k: kinds[k]["ms"])
+    dom = max((k for k in kinds if k != "svd_fp64"), key=lambda k: kinds[k]["ms"])
     line["roofline"] = roofline(dom, kinds[dom], P, args.mode, pc)
     line["roofline_gemm"] = roofline("gemm", kinds["gemm"], P, args.mode, pc)
     line["kernel_time_ms"] = {k: round(v["ms"], 1) for k, v in kinds.items()}
@@ -780,7 +790,14 @@ def cylinder_main(args, rank, world, local):
     if args.mode != "f64" and args.compare_f64:
         n = max(1, min(args.compare_sweeps, args.steps))
         lf = state_log(q)
+        q.stats.reset()
+        q.stats.enable(True)
         _, _, S64 = sweeps_call(q, mpo, S0, n, "f64", args.D, lf)
+        k64 = {k: q.stats.get(k) for k in q.stats.KINDS}
+        q.stats.enable(False)
+        # the plain path against its own roofline: FP64 GEMMs and FP64 Jacobi against cuBLAS DGEMM
+        line["roofline_f64"] = {k: roofline(k, k64[k], P, "f64", pc) for k in ("gemm", "svd")}
+        line["kernel_time_ms_f64"] = {k: round(v["ms"], 1) for k, v in k64.items()}
         t64 = lf.time_list[1:] if len(lf.time_list) > 1 else lf.time_list
         tm = log.time_list[1:] if len(log.time_list) > 1 else log.time_list
         Sm = log.kept if log.kept is not None else S_mix
@@ -835,8 +852,8 @@ def main():
     rank, world, local = dist_env()
     hub = args.model == "hubbard"
     cyl = args.model == "cylinder"
-    if cyl and args.workload in ("svd", "contraction"):
-        args.model, cyl = "heisenberg", False   # these workloads take a chain's theta or the theta pair
+    if cyl and args.workload == "contraction":
+        args.model, cyl = "heisenberg", False   # the theta-pair microbench
     if args.L is None:
         args.L = 72 if cyl else (64 if hub else 32)
     if args.D is None:
@@ -950,7 +967,7 @@ def main():
     e2e = e2e_sweep(q, mpo, mps1, args)
     P = peaks()
     pc = {}
-    dom = max(kinds, key=lambda k: kinds[k]["ms"])
+    dom = max((k for k in kinds if k != "svd_fp64"), key=lambda k: kinds[k]["ms"])
     line = {"metric": METRIC, "value": job_per_sweep, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f64svd+f64",

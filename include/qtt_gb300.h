@@ -283,7 +283,9 @@ int qtt_svd_dense_noalloc(const double *a, int64_t m, int64_t n, double *u, doub
 /* ------------------------------------------------------------------ measurement */
 /* Per-kernel-class device time (CUDA events on the launching stream) and
  * algorithmic work: kind 0 block GEMM (FLOP), 1 permute (bytes), 2 sector SVD
- * (FLOP, one-sided Jacobi estimate), 3 elementwise (bytes), 4 sector pack (bytes). */
+ * (FLOP, LAPACK-class count 4p^2q + 8pq^2 + 9q^3 per p x q sector), 3 elementwise (bytes),
+ * 4 sector pack (bytes), 5 the FP64 stage of the mixed path's sector SVDs (time only; part
+ * of kind 2). */
 int qtt_stats_enable(int on);
 int qtt_stats_reset(void);
 int qtt_stats_get(int kind, double *ms, double *work, int64_t *launches);

@@ -58,7 +58,7 @@ def set_jacobi_kernel(which):
 
 class stats:
     """Per-kernel-class device time (CUDA events) and algorithmic work."""
-    KINDS = {"gemm": 0, "permute": 1, "svd": 2, "elementwise": 3, "pack": 4}
+    KINDS = {"gemm": 0, "permute": 1, "svd": 2, "elementwise": 3, "pack": 4, "svd_fp64": 5}
 
     @staticmethod
     def enable(on=True):

@@ -205,6 +205,8 @@ void launch_warm_apply(void *work, void *rot, void *tmp, const WarmDesc *wd, int
 // The FP64 Jacobi then runs warm on (w1, vb).
 void launch_svd_refine(const float *rot32, const double *w64, double *w1, double *va, double *vb, double *g,
                        const std::vector<SectorDesc> &secs);
+// out[s_off + j] = squared norm of column j of every sector (FP64 work matrices)
+void launch_col_norms(const double *W, const SectorDesc *secs, int nsec, int max_q, double *out);
 // Segment = one input block (rows x cols at src_off) placed at rows [r0, r0+rows),
 // cols [c0, c0+cols) of sector `sector`.
 struct PackEntry {

@@ -158,6 +158,13 @@ struct TruncHint {
     bool active = false;
     int64_t min_size = 0;
     WarmStart *ws = nullptr;  // warm starts of the decomposition (svd only)
+    // the truncation that follows (tol, max_size, pow), for the mixed path's estimate of
+    // its threshold; discard_tau receives the largest column norm that left the FP64
+    // sweeps as "below the threshold" (0: none), allow_discard switches that off
+    double tol = 0.0, pw = 2.0;
+    int64_t max_size = 0;
+    bool allow_discard = true;
+    double discard_tau = 0.0;
 };
 TruncHint &trunc_hint() {
     thread_local TruncHint h;
@@ -165,12 +172,29 @@ TruncHint &trunc_hint() {
 }
 struct ScopedTruncHint {
     TruncHint saved;
-    ScopedTruncHint(bool on, int64_t min_size, WarmStart *ws)
-        : saved(trunc_hint()) {
-        trunc_hint() = TruncHint{on, min_size, ws};
-    }
+    ScopedTruncHint(const TruncHint &h) : saved(trunc_hint()) { trunc_hint() = h; }
     ~ScopedTruncHint() { trunc_hint() = saved; }
 };
+
+// The smallest value truncate_impl keeps (btensor_linalg.cpp:658-682,
+// LinearAlgebra.cpp:57-75) among `vals` sorted descending, less the 2 eps slack; -1 when
+// there are none.
+double kept_threshold(const std::vector<double> &sorted, double tol, double pw, int64_t min_size, int64_t max_size) {
+    const int64_t n = int64_t(sorted.size());
+    if (n == 0) return -1.0;
+    const double toln = std::pow(tol, pw);
+    int64_t last = n - 1;
+    double trunc = std::pow(std::fabs(sorted[last]), pw);
+    // `last_index >= min_size` compares a signed index with an unsigned size
+    while (uint64_t(last) >= uint64_t(min_size)) {
+        if (trunc > toln && last < max_size) break;
+        --last;
+        int64_t li = last < 0 ? last + n : last;  // negative indices wrap like tensor.index
+        trunc += std::pow(std::fabs(sorted[li]), pw);
+    }
+    double smallest = sorted[last < 0 ? last + n : last];
+    return smallest - 2.0 * smallest * 2.220446049250313e-16;
+}
 constexpr double kDeflateF32 = 1.1920928955078125e-07;  // FP32 epsilon (2^-23)
 constexpr double kDeflateF64 = 8.0 * 2.220446049250313e-16;  // 8 x FP64 epsilon (2^-49)
 
@@ -348,6 +372,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
         const void *fw = W, *fr = D.rot->p;
         BufPtr w64, w1, va, vbuf, gbuf, ibuf64;
         if (f32) {
+            StatScope sc64(ST_SVD64, 0.0);
             // FP64 stage: the FP64 sector matrices, the FP32 rotations made orthogonal in
             // FP64, W1 = W V, and FP64 Jacobi sweeps from that warm start
             w64 = dev_alloc(size_t(std::max<int64_t>(wtot, 1)) * 8);
@@ -371,8 +396,54 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             BufPtr thr64;
             dnorm.reset();
             if (deflate) deflation(w1->p, 0, thr64, dnorm);
-            launch_jacobi(w1->p, vbuf->p, dsec64, dslots, nsec, max_steps, max_sweeps, sw64, sw64 + nsec, 0, max_p,
-                          stot, vwork64->p, vb64, deflate ? thr64->p : nullptr, deflate ? dnorm->p : nullptr);
+            auto fp64_sweeps = [&](int cap_sweeps, const void *thr) {
+                launch_jacobi(w1->p, vbuf->p, dsec64, dslots, nsec, max_steps, cap_sweeps, sw64, sw64 + nsec, 0,
+                              max_p, stot, vwork64->p, vb64, deflate ? thr : nullptr, deflate ? dnorm->p : nullptr);
+            };
+            // The FP32 sweeps resolved every value above FP32 resolution.  When the truncation
+            // that follows keeps only values well above that, one FP64 sweep decouples the
+            // columns, and the columns below half the truncation threshold (estimated from
+            // the column norms) then leave the FP64 sweeps with the null ones: they are
+            // never kept, and no value above the threshold can hide among them.
+            TruncHint &th = trunc_hint();
+            BufPtr thr_discard;
+            if (deflate && th.allow_discard && th.max_size > 0) {
+                fp64_sweeps(1, thr64->p);
+                BufPtr cn = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * 8);
+                launch_col_norms(static_cast<const double *>(w1->p), dsec64, nsec, max_q,
+                                 static_cast<double *>(cn->p));
+                std::vector<double> n2(size_t(std::max<int64_t>(stot, 1)));
+                cuda_check(cudaMemcpyAsync(n2.data(), cn->p, size_t(stot) * 8, cudaMemcpyDeviceToHost, ctx().stream),
+                           "cudaMemcpyAsync(column norms)");
+                cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+                std::vector<double> vals(n2.begin(), n2.begin() + stot);
+                for (double &x : vals) x = std::sqrt(std::max(x, 0.0));
+                std::sort(vals.begin(), vals.end(), std::greater<double>());
+                const double t_est = kept_threshold(vals, th.tol, th.pw, th.min_size, th.max_size);
+                std::vector<double> thr(nsec, 0.0);
+                double tau_max = 0.0;
+                for (int i = 0; i < nsec; ++i) {
+                    const SectorDesc &d = D.desc[i];
+                    double f2 = 0.0;
+                    for (int j = 0; j < d.q; ++j) f2 += n2[d.s_off + j];
+                    const double null2 = kDeflateF64 * kDeflateF64 * f2;
+                    const double tau = 0.5 * t_est;
+                    if (t_est > 0.0 && tau > 64.0 * kDeflateF32 * std::sqrt(f2)) {
+                        thr[i] = std::max(null2, tau * tau);
+                        tau_max = std::max(tau_max, tau);
+                    } else {
+                        thr[i] = null2;
+                    }
+                }
+                if (tau_max > 0.0) {
+                    th.discard_tau = std::max(th.discard_tau, tau_max);
+                    thr_discard = dev_alloc(size_t(nsec) * 8);
+                    cuda_check(cudaMemcpyAsync(thr_discard->p, upload(thr.data(), thr.size() * 8),
+                                               size_t(nsec) * 8, cudaMemcpyDeviceToDevice, ctx().stream),
+                               "cudaMemcpyAsync(thresholds)");
+                }
+            }
+            fp64_sweeps(max_sweeps, thr_discard ? thr_discard->p : (thr64 ? thr64->p : nullptr));
             fw = w1->p;
             fr = vbuf->p;
         }
@@ -640,18 +711,7 @@ SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, dou
     std::sort(sorted.begin(), sorted.end(), std::greater<double>());
     const int64_t n = int64_t(sorted.size());
     if (n == 0) return std::move(in);
-    const double toln = std::pow(tol, pw);
-    int64_t last = n - 1;
-    double trunc = std::pow(std::fabs(sorted[last]), pw);
-    // `last_index >= min_size` compares a signed index with an unsigned size
-    while (uint64_t(last) >= uint64_t(min_size)) {
-        if (trunc > toln && last < max_size) break;
-        --last;
-        int64_t li = last < 0 ? last + n : last;  // negative indices wrap like tensor.index
-        trunc += std::pow(std::fabs(sorted[li]), pw);
-    }
-    double smallest = sorted[last < 0 ? last + n : last];
-    smallest -= 2.0 * smallest * 2.220446049250313e-16;
+    const double smallest = kept_threshold(sorted, tol, pw, min_size, max_size);
     double dropped = 0.0, total = 0.0;
     for (double v : sorted) {
         const double w = std::pow(std::fabs(v), pw);
@@ -713,17 +773,36 @@ SVDOut truncate(SVDOut &&in, int64_t max_size, int64_t min_size, double tol, dou
     o.d = dd;
     o.discarded = dropped;
     o.total = total;
+    o.kept_min = smallest;
     return o;
 }
 
 SVDOut svd_truncated(const BT &t, int64_t split, double tol, int64_t min_size, int64_t max_size, double pw,
                      WarmStart *ws) {
+    TruncHint h;
+    h.active = tol > 0.0;
+    h.min_size = min_size;
+    h.ws = ws;
+    h.tol = tol;
+    h.pw = pw;
+    h.max_size = max_size;
     SVDOut full;
+    double tau = 0.0;
     {
-        ScopedTruncHint hint(tol > 0.0, min_size, ws);
+        ScopedTruncHint hint(h);
         full = svd_split(t, split);
+        tau = trunc_hint().discard_tau;
     }
-    return truncate(std::move(full), max_size, min_size, tol, pw, true);
+    SVDOut out = truncate(std::move(full), max_size, min_size, tol, pw, true);
+    if (tau > 0.0 && !(out.kept_min > tau)) {
+        // the truncation reaches down to columns the FP64 sweeps left unresolved as
+        // below its estimated threshold: decompose again, resolving every column
+        h.allow_discard = false;
+        ScopedTruncHint hint(h);
+        full = svd_split(t, split);
+        out = truncate(std::move(full), max_size, min_size, tol, pw, true);
+    }
+    return out;
 }
 
 // eigh(btensor, upper), btensor_linalg.cpp:294-368 (eigenvalues ascending per sector)

@@ -316,6 +316,7 @@ struct SVDOut {
     // after a truncation: sum of |s|^pow over the dropped values and over all values
     // (the discarded weight truncate_impl bounds by tol^pow, btensor_linalg.cpp:658-682)
     double discarded = 0.0, total = 0.0;
+    double kept_min = -1.0;  // the smallest value the truncation keeps, less its 2 eps slack
 };
 SVDOut svd(const BT &t);                       // untruncated, rank >= 2, sectors on the last two legs
 SVDOut svd_split(const BT &t, int64_t split);  // svd(A, split)
@@ -387,7 +388,8 @@ inline void tc_error_raise() {
 // ---------------------------------------------------------------- timing statistics
 // Per-kernel-class device time measured with CUDA events on the launching stream,
 // plus the algorithmic work each launch did (FLOPs or bytes).
-enum StatKind : int { ST_GEMM = 0, ST_PERMUTE = 1, ST_SVD = 2, ST_ELEMWISE = 3, ST_PACK = 4, ST_COUNT = 5 };
+// ST_SVD64: the FP64 stage of the mixed path's sector SVDs (a part of ST_SVD's time)
+enum StatKind : int { ST_GEMM = 0, ST_PERMUTE = 1, ST_SVD = 2, ST_ELEMWISE = 3, ST_PACK = 4, ST_SVD64 = 5, ST_COUNT = 6 };
 void stats_enable(bool on);
 bool stats_enabled();
 // Work known only after the kernels ran (e.g. Jacobi sweeps): resolved when read.

@@ -128,7 +128,28 @@ void secgemm(const TA *A, const TB *B, double *C, std::vector<SecGemm> &tasks, c
     cuda_check(cudaGetLastError(), "sector GEMM launch");
 }
 
+// Squared column norms of every sector matrix (one warp per column).
+__global__ void k_col_norms(const double *__restrict__ W, const SectorDesc *__restrict__ secs,
+                            double *__restrict__ out) {
+    const SectorDesc sd = secs[blockIdx.y];
+    const int lane = threadIdx.x & 31;
+    const int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (col >= sd.q) return;
+    const double *w = W + sd.w_off + int64_t(col) * sd.p;
+    double acc = 0.0;
+    for (int r = lane; r < sd.p; r += 32) acc = fma(w[r], w[r], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[sd.s_off + col] = acc;
+}
+
 }  // namespace
+
+void launch_col_norms(const double *W, const SectorDesc *secs, int nsec, int max_q, double *out) {
+    if (nsec <= 0 || max_q <= 0) return;
+    k_col_norms<<<dim3(unsigned((max_q + 7) / 8), unsigned(nsec)), 256, 0, ctx().stream>>>(W, secs, out);
+    count_launch();
+    cuda_check(cudaGetLastError(), "column norm launch");
+}
 
 void launch_svd_refine(const float *rot32, const double *w64, double *w1, double *va, double *vb, double *g,
                        const std::vector<SectorDesc> &secs) {
