@@ -61,6 +61,11 @@ def parse():
     p.add_argument("--compare-sweeps", type=int, default=2,
                    help="cylinder: FP64 sweeps from the timed state for vs_fp64")
     p.add_argument("--ramp-sweeps", type=int, default=2, help="cylinder: sweeps at each ramp bond dimension")
+    p.add_argument("--ramp-lanczos", type=int, default=4,
+                   help="cylinder: Lanczos steps per bond in the ramp sweeps (state preparation only; the "
+                        "warm-up and timed sweeps use QuantiT's one-step update)")
+    p.add_argument("--converge-sweeps", type=int, default=2,
+                   help="cylinder: ramp-style sweeps at D before the warm-up (state preparation)")
     p.add_argument("--e2e-steps", type=int, default=2, help="cylinder: sweeps timed through the public API")
     p.add_argument("--cpu-bonds", type=int, default=6, help="cylinder: bonds of the stratified CPU sample")
     p.add_argument("--cpu-steps", type=int, default=3, help="cylinder: CPU bond updates in our arm's cpu_baseline")
@@ -530,13 +535,15 @@ def cylinder_mpo(q):
     return q.networks.cylinder_heisenberg(CYL_LX, CYL_LY, 1.0, "snake", compress=True)
 
 
-def sweeps_call(q, mpo, mps, n, mode, D, logger=None):
-    """ONE dmrg call of n sweeps from mps (QuantiT's update, cutoff 1e-10, max bond D),
-    timed with CUDA events on the library stream: (seconds, energy, final state)."""
+def sweeps_call(q, mpo, mps, n, mode, D, logger=None, lanczos=1):
+    """ONE dmrg call of n sweeps from mps (QuantiT's update, cutoff 1e-10, max bond D;
+    lanczos > 1: k-step Lanczos instead), timed with CUDA events on the library stream:
+    (seconds, energy, final state)."""
     import torch
     stream = torch.cuda.ExternalStream(q.lib().qtt_get_stream())
     opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=0.0, max_bond=D, min_bond=4,
-                                     maximum_iterations=n, gemm=mode, final_energy_fp64=False)
+                                     maximum_iterations=n, gemm=mode, final_energy_fp64=False,
+                                     lanczos_steps=lanczos)
     cur = q.networks.bMPS(list(mps), mps.orthogonality_center)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -570,11 +577,13 @@ def prepare_cylinder(q, args, seed):
     mps.move_oc(0)
     mps.normalize_center()
     info = {"ramp": []}
-    for Dr in RAMP:
-        if Dr >= args.D:
-            break
-        t, E, mps = sweeps_call(q, mpo, mps, args.ramp_sweeps, args.mode, Dr)
-        info["ramp"].append({"D": Dr, "sweeps": args.ramp_sweeps, "s": round(t, 2), "ritz_E": E})
+    stages = [(Dr, args.ramp_sweeps) for Dr in RAMP if Dr < args.D] + [(args.D, args.converge_sweeps)]
+    for Dr, n in stages:
+        if n <= 0:
+            continue
+        t, E, mps = sweeps_call(q, mpo, mps, n, args.mode, Dr, lanczos=args.ramp_lanczos)
+        info["ramp"].append({"D": Dr, "sweeps": n, "lanczos_steps": args.ramp_lanczos, "s": round(t, 2),
+                             "E": E})
     log = state_log(q)
     t, E, mps = sweeps_call(q, mpo, mps, max(args.warmup, 1), args.mode, args.D, log)
     info["warmup"] = {"sweeps": max(args.warmup, 1), "s": round(t, 2), "ritz_E": log.energies,
@@ -673,8 +682,9 @@ def cylinder_config(args):
             "model": "spin-1/2 Heisenberg J=1 on an open cylinder of length 12 and circumference 6 "
                      "(periodic), snake-ordered MPO compressed to its Schmidt rank (bond dimension 20)",
             "cutoff": 1e-10, "update": "one-step Lanczos (QuantiT two_sites_update)",
-            "start": f"random_bMPS(256, seed={args.seed}), {args.ramp_sweeps} sweeps per ramp stage, "
-                     f"{args.warmup} warm-up sweeps at D",
+            "start": f"random_bMPS(256, seed={args.seed}); {args.ramp_sweeps} sweeps per ramp stage and "
+                     f"{args.converge_sweeps} at D with {args.ramp_lanczos}-step Lanczos (state preparation); "
+                     f"{args.warmup} warm-up sweeps at D with the timed update",
             "l2": "working set (MPS + environments, GBs) far larger than L2 (129 MB)"}
 
 
@@ -687,7 +697,8 @@ def reference_arm_cylinder(args, cfg):
     d = tempfile.mkdtemp(prefix="qtt_cpu_sample_")
     try:
         cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--prepare-cpu-sample", d, "--D", str(args.D),
-               "--warmup", str(args.warmup), "--ramp-sweeps", str(args.ramp_sweeps), "--cpu-bonds",
+               "--warmup", str(args.warmup), "--ramp-sweeps", str(args.ramp_sweeps), "--ramp-lanczos",
+               str(args.ramp_lanczos), "--converge-sweeps", str(args.converge_sweeps), "--cpu-bonds",
                str(args.cpu_bonds), "--mode", args.mode, "--seed", str(args.seed)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

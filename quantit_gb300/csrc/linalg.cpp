@@ -401,7 +401,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
                               max_p, stot, vwork64->p, vb64, deflate ? thr : nullptr, deflate ? dnorm->p : nullptr);
             };
             // The FP32 sweeps resolved every value above FP32 resolution.  When the truncation
-            // that follows keeps only values well above that, one FP64 sweep decouples the
+            // that follows keeps only values above that (8 eps32 ||W||), one FP64 sweep decouples the
             // columns, and the columns below half the truncation threshold (estimated from
             // the column norms) then leave the FP64 sweeps with the null ones: they are
             // never kept, and no value above the threshold can hide among them.
@@ -428,7 +428,10 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
                     for (int j = 0; j < d.q; ++j) f2 += n2[d.s_off + j];
                     const double null2 = kDeflateF64 * kDeflateF64 * f2;
                     const double tau = 0.5 * t_est;
-                    if (t_est > 0.0 && tau > 64.0 * kDeflateF32 * std::sqrt(f2)) {
+                    // a column of norm >= 4 eps32 ||W|| carries FP32 rounding noise of at most a
+                    // quarter of itself: FP32 sweeps left no value above 2 tau spread over such
+                    // columns (the truncation is checked against tau all the same)
+                    if (t_est > 0.0 && tau > 4.0 * kDeflateF32 * std::sqrt(f2)) {
                         thr[i] = std::max(null2, tau * tau);
                         tau_max = std::max(tau_max, tau);
                     } else {
