@@ -166,6 +166,8 @@ struct JacobiParams {
     int *rotated;  // nsec * max_sweeps flags, zero on entry: a rotation happened in (sector, sweep)
     const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
     T *dnorm;      // per column (s_off + column): squared norm when deflated, 0 otherwise
+    const T *skip; // per sector (null: none): a pair whose squared norms are both below it is
+                   // left as it is (both columns lie below what the caller keeps)
 };
 
 // Rotation of one column pair by one warp.  With R > 0 (p <= 32 R) every lane
@@ -177,7 +179,8 @@ struct JacobiParams {
 // Returns whether a column was rotated or deflated.
 template <class T, int R>
 __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ wb, T *__restrict__ va,
-                                            T *__restrict__ vb, int p, int q, int lane, T thr, T *da, T *db) {
+                                            T *__restrict__ vb, int p, int q, int lane, T thr, T *da, T *db,
+                                            T skip) {
     T al = 0, be = 0, ga = 0;
     T x[R > 0 ? R : 1], y[R > 0 ? R : 1];
     if (R > 0) {
@@ -216,6 +219,7 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
         }
         return true;
     }
+    if (al < skip && be < skip) return false;
     if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
     T sn, tau;
     rot_params(al, be, ga, sn, tau);
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
             T *vb = P.rot + sd.rot_off + int64_t(b) * sd.q;
             T *dn = P.dnorm ? P.dnorm + sd.s_off : nullptr;
             if (!rotate_pair<T, R>(wa, wb, va, vb, sd.p, sd.q, lane, P.defl ? P.defl[s] : T(0), dn ? dn + a : nullptr,
-                                   dn ? dn + b : nullptr))
+                                   dn ? dn + b : nullptr, P.skip ? P.skip[s] : T(0)))
                 continue;
             if (lane == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
         }
@@ -386,6 +390,8 @@ struct BJacobiParams {
     int max_q;     // widest sector (columns)
     const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
     T *dnorm;      // per column (s_off + column): squared norm when deflated, 0 otherwise
+    const T *skip; // per sector (null: none): a pair whose squared norms are both below it is
+                   // left as it is (both columns lie below what the caller keeps)
 };
 
 __device__ __forceinline__ int bj_items(int q, int B) {
@@ -478,8 +484,9 @@ __device__ __forceinline__ void bj_params_fast(float al, float be, float ga, flo
 // (set to zero, norm 0; dx / dy receive its squared norm before, else stay 0).
 template <class T, int R>
 __device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T thr, T &sn, T &tau, T &dx,
-                                          T &dy) {
+                                          T &dy, T skip) {
     if (al == T(0) || be == T(0)) return false;
+    if (al < skip && be < skip) return false;
     const T ga = bj_dot(x, y);
     if (ga == T(0)) return false;
     T t;
@@ -674,6 +681,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             T *V = P.rot + sd.rot_off;
             const T tol = Eps<T>::tol(p);
             const T thr = P.defl ? P.defl[s] : T(0);
+            const T skp = P.skip ? P.skip[s] : T(0);
             bool zeroed = false;
 
             for (int j = warp; j < NP; j += B) {
@@ -720,7 +728,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                         bj_load(x, cols + u * PP, lane);
                         bj_load(y, cols + v * PP, lane);
                         T al = nrm[u], be = nrm[v], dx = T(0), dy = T(0);
-                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy)) {
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy, skp)) {
                             if (lane == 0 && dx > T(0)) P.dnorm[sd.s_off + column(u)] = dx;
                             if (lane == 0 && dy > T(0)) P.dnorm[sd.s_off + column(v)] = dy;
                             bj_store(x, cols + u * PP, lane);
@@ -756,7 +764,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     if (mine && valid(j)) {
                         bj_load(y, cols + j * PP, lane);
                         T be = nrm[j], dx = T(0), dy = T(0);
-                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy)) {
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy, skp)) {
                             if (lane == 0 && dx > T(0)) P.dnorm[sd.s_off + column(warp)] = dx;
                             if (lane == 0 && dy > T(0)) P.dnorm[sd.s_off + column(j)] = dy;
                             bj_store(y, cols + j * PP, lane);
@@ -1284,7 +1292,7 @@ void tune_save(const TuneKey &k, int w) {
 template <class T>
 void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, int nsec, int max_steps_per_sweep,
                  int max_sweeps, int *sweeps_out, int *flags, int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes,
-                 const T *defl, T *dnorm, cudaStream_t stream, bool tune) {
+                 const T *defl, T *dnorm, cudaStream_t stream, bool tune, const T *skip) {
     if (nsec > 12 * 1024) fail(ERR_INVALID_ARGUMENT, "too many sectors for one decomposition launch");
     const size_t smem = size_t(2 * nsec) * sizeof(int);
     cuda_check(cudaMemsetAsync(flags, 0, size_t(nsec) * max_sweeps * sizeof(int), stream), "memset flags");
@@ -1300,6 +1308,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
         B.rotated = flags;
         B.defl = defl;
         B.dnorm = dnorm;
+        B.skip = skip;
         B.max_q = max_steps_per_sweep + 1;  // the widest sector's even column count bounds q
         const bool f32 = sizeof(T) == 4;
         const std::vector<int> cands = block_widths(f32, r_class(max_p));
@@ -1362,6 +1371,7 @@ void jacobi_impl(T *work, T *rot, const SectorDesc *sec, const int *slot_start, 
     P.rotated = flags;
     P.defl = defl;
     P.dnorm = dnorm;
+    P.skip = skip;
     const int64_t pairs = (sum_q + nsec) / 2 + nsec;  // pairs per step, an upper bound
     // registers per lane: the longest column over the sectors decides
     if (max_p <= 4 * 32)
@@ -1426,24 +1436,26 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
                       int max_p, int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm,
-                      bool tune) {
+                      bool tune, const void *skip) {
     if (nsec <= 0) return;
     if ((defl == nullptr) != (dnorm == nullptr)) fail(ERR_INVALID_ARGUMENT, "deflation needs thresholds and norms");
     if (f32)
         jacobi_impl(static_cast<float *>(work), static_cast<float *>(rot), sec, slot_start, nsec, max_steps_per_sweep,
                     max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
-                    static_cast<const float *>(defl), static_cast<float *>(dnorm), stream, tune);
+                    static_cast<const float *>(defl), static_cast<float *>(dnorm), stream, tune,
+                    static_cast<const float *>(skip));
     else
         jacobi_impl(static_cast<double *>(work), static_cast<double *>(rot), sec, slot_start, nsec,
                     max_steps_per_sweep, max_sweeps, sweeps_out, flags, max_p, sum_q, vwork, vwork_bytes,
-                    static_cast<const double *>(defl), static_cast<double *>(dnorm), stream, tune);
+                    static_cast<const double *>(defl), static_cast<double *>(dnorm), stream, tune,
+                    static_cast<const double *>(skip));
 }
 
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
-                   int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm) {
+                   int64_t sum_q, void *vwork, size_t vwork_bytes, const void *defl, void *dnorm, const void *skip) {
     launch_jacobi_on(ctx().stream, work, rot, sec, slot_start, nsec, max_steps_per_sweep, max_sweeps, sweeps_out, flags,
-                     f32, max_p, sum_q, vwork, vwork_bytes, defl, dnorm);
+                     f32, max_p, sum_q, vwork, vwork_bytes, defl, dnorm, true, skip);
 }
 
 void launch_warm_apply(void *work, void *rot, void *tmp, const WarmDesc *wd, int nwarm, int ntiles, int f32) {

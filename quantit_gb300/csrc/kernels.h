@@ -205,8 +205,9 @@ void launch_warm_apply(void *work, void *rot, void *tmp, const WarmDesc *wd, int
 // The FP64 Jacobi then runs warm on (w1, vb).
 void launch_svd_refine(const float *rot32, const double *w64, double *w1, double *va, double *vb, double *g,
                        const std::vector<SectorDesc> &secs);
-// out[s_off + j] = squared norm of column j of every sector (FP64 work matrices)
-void launch_col_norms(const double *W, const SectorDesc *secs, int nsec, int max_q, double *out);
+// out[s_off + j] = squared norm (FP64) of column j of every sector's work matrix (f32:
+// FP32 work matrices)
+void launch_col_norms(const void *W, const SectorDesc *secs, int nsec, int max_q, double *out, int f32);
 // Segment = one input block (rows x cols at src_off) placed at rows [r0, r0+rows),
 // cols [c0, c0+cols) of sector `sector`.
 struct PackEntry {
@@ -232,10 +233,12 @@ void launch_eigh_prepare(void *work, SectorDesc *sec, int nsec, int upper, int f
 // defl (optional, launch_deflation_thresholds, the work type): per sector, a column
 // whose squared norm falls to the threshold or below is set to zero and leaves the
 // sweeps (a numerically zero column); null: no deflation.
+// skip (optional, the work type): per sector, a pair whose squared column norms are both
+// below it is not rotated (columns the caller will discard).
 void launch_jacobi(void *work, void *rot, const SectorDesc *sec, const int *slot_start, int nsec,
                    int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32, int max_p,
                    int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0, const void *defl = nullptr,
-                   void *dnorm = nullptr);
+                   void *dnorm = nullptr, const void *skip = nullptr);
 // thr[s] <- delta^2 ||W_s||_F^2 for every svd sector (0 for eigh), in the work type.
 void launch_deflation_thresholds(const void *work, const SectorDesc *sec, int nsec, double delta, void *thr, int f32);
 // dnorm (with defl; the work type, sum of q entries at s_off, zero on entry) receives
@@ -258,7 +261,8 @@ void launch_finish(const void *work, const void *rot, double *U, double *V, doub
 void launch_jacobi_on(cudaStream_t stream, void *work, void *rot, const SectorDesc *sec, const int *slot_start,
                       int nsec, int max_steps_per_sweep, int max_sweeps, int *sweeps_out, int *flags, int f32,
                       int max_p, int64_t sum_q, void *vwork = nullptr, size_t vwork_bytes = 0,
-                      const void *defl = nullptr, void *dnorm = nullptr, bool tune = true);
+                      const void *defl = nullptr, void *dnorm = nullptr, bool tune = true,
+                      const void *skip = nullptr);
 void launch_finish_on(cudaStream_t stream, const void *work, const void *rot, double *U, double *V, double *s,
                       const SectorDesc *sec, int nsec, int max_q, double *scratch, int f32, int complete_cap = -1,
                       const void *dnorm = nullptr, int *dpos = nullptr, int *perm_out = nullptr,

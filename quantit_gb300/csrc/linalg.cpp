@@ -371,6 +371,45 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
                       vwork->p, vb, deflate ? thr->p : nullptr, deflate ? dnorm->p : nullptr);
         const void *fw = W, *fr = D.rot->p;
         BufPtr w64, w1, va, vbuf, gbuf, ibuf64;
+        // The FP32 sweeps resolved every value above FP32 resolution.  When the truncation
+        // that follows keeps only values above 8 eps32 ||W_s|| (its threshold estimated from
+        // the FP32 column norms with truncate's own rule), the FP64 sweeps may leave the
+        // columns below tau = half that threshold unresolved among themselves: they are never
+        // kept, and no value above the threshold can hide among them -- a column of norm
+        // >= 4 eps32 ||W_s|| carries FP32 rounding noise of at most a quarter of itself.  The
+        // truncation is checked against tau all the same (svd_truncated).
+        std::vector<double> discard, null2;
+        TruncHint &th = trunc_hint();
+        if (f32 && deflate && th.allow_discard && th.max_size > 0) {
+            BufPtr cn = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * 8);
+            launch_col_norms(W, dsec, nsec, max_q, static_cast<double *>(cn->p), 1);
+            std::vector<double> n2(size_t(std::max<int64_t>(stot, 1)));
+            cuda_check(cudaMemcpyAsync(n2.data(), cn->p, size_t(stot) * 8, cudaMemcpyDeviceToHost, ctx().stream),
+                       "cudaMemcpyAsync(column norms)");
+            cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+            std::vector<double> vals(n2.begin(), n2.begin() + stot);
+            for (double &x : vals) x = std::sqrt(std::max(x, 0.0));
+            std::sort(vals.begin(), vals.end(), std::greater<double>());
+            const double t_est = kept_threshold(vals, th.tol, th.pw, th.min_size, th.max_size);
+            discard.assign(nsec, 0.0);
+            null2.assign(nsec, 0.0);
+            double tau_max = 0.0;
+            for (int i = 0; i < nsec; ++i) {
+                const SectorDesc &d = D.desc[i];
+                double f2 = 0.0;
+                for (int j = 0; j < d.q; ++j) f2 += n2[d.s_off + j];
+                null2[i] = kDeflateF64 * kDeflateF64 * f2;
+                const double tau = 0.5 * t_est;
+                if (t_est > 0.0 && tau > 4.0 * kDeflateF32 * std::sqrt(f2)) {
+                    discard[i] = tau;
+                    tau_max = std::max(tau_max, tau);
+                }
+            }
+            if (tau_max > 0.0)
+                th.discard_tau = std::max(th.discard_tau, tau_max);
+            else
+                discard.clear();
+        }
         if (f32) {
             StatScope sc64(ST_SVD64, 0.0);
             // FP64 stage: the FP64 sector matrices, the FP32 rotations made orthogonal in
@@ -396,57 +435,26 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             BufPtr thr64;
             dnorm.reset();
             if (deflate) deflation(w1->p, 0, thr64, dnorm);
-            auto fp64_sweeps = [&](int cap_sweeps, const void *thr) {
+            auto fp64_sweeps = [&](int cap_sweeps, const void *thr, const void *skip) {
                 launch_jacobi(w1->p, vbuf->p, dsec64, dslots, nsec, max_steps, cap_sweeps, sw64, sw64 + nsec, 0,
-                              max_p, stot, vwork64->p, vb64, deflate ? thr : nullptr, deflate ? dnorm->p : nullptr);
+                              max_p, stot, vwork64->p, vb64, deflate ? thr : nullptr, deflate ? dnorm->p : nullptr,
+                              skip);
             };
-            // The FP32 sweeps resolved every value above FP32 resolution.  When the truncation
-            // that follows keeps only values above that (8 eps32 ||W||), one FP64 sweep decouples the
-            // columns, and the columns below half the truncation threshold (estimated from
-            // the column norms) then leave the FP64 sweeps with the null ones: they are
-            // never kept, and no value above the threshold can hide among them.
-            TruncHint &th = trunc_hint();
-            BufPtr thr_discard;
-            if (deflate && th.allow_discard && th.max_size > 0) {
-                fp64_sweeps(1, thr64->p);
-                BufPtr cn = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * 8);
-                launch_col_norms(static_cast<const double *>(w1->p), dsec64, nsec, max_q,
-                                 static_cast<double *>(cn->p));
-                std::vector<double> n2(size_t(std::max<int64_t>(stot, 1)));
-                cuda_check(cudaMemcpyAsync(n2.data(), cn->p, size_t(stot) * 8, cudaMemcpyDeviceToHost, ctx().stream),
-                           "cudaMemcpyAsync(column norms)");
-                cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
-                std::vector<double> vals(n2.begin(), n2.begin() + stot);
-                for (double &x : vals) x = std::sqrt(std::max(x, 0.0));
-                std::sort(vals.begin(), vals.end(), std::greater<double>());
-                const double t_est = kept_threshold(vals, th.tol, th.pw, th.min_size, th.max_size);
-                std::vector<double> thr(nsec, 0.0);
-                double tau_max = 0.0;
+            if (discard.empty()) {
+                fp64_sweeps(max_sweeps, thr64 ? thr64->p : nullptr, nullptr);
+            } else {
+                // one sweep decouples the columns (pairs of two discarded columns stay as they
+                // are), then the columns below tau leave the sweeps with the null ones
+                std::vector<double> skip2(nsec), thr2(nsec);
                 for (int i = 0; i < nsec; ++i) {
-                    const SectorDesc &d = D.desc[i];
-                    double f2 = 0.0;
-                    for (int j = 0; j < d.q; ++j) f2 += n2[d.s_off + j];
-                    const double null2 = kDeflateF64 * kDeflateF64 * f2;
-                    const double tau = 0.5 * t_est;
-                    // a column of norm >= 4 eps32 ||W|| carries FP32 rounding noise of at most a
-                    // quarter of itself: FP32 sweeps left no value above 2 tau spread over such
-                    // columns (the truncation is checked against tau all the same)
-                    if (t_est > 0.0 && tau > 4.0 * kDeflateF32 * std::sqrt(f2)) {
-                        thr[i] = std::max(null2, tau * tau);
-                        tau_max = std::max(tau_max, tau);
-                    } else {
-                        thr[i] = null2;
-                    }
+                    skip2[i] = discard[i] * discard[i];
+                    thr2[i] = std::max(null2[i], skip2[i]);
                 }
-                if (tau_max > 0.0) {
-                    th.discard_tau = std::max(th.discard_tau, tau_max);
-                    thr_discard = dev_alloc(size_t(nsec) * 8);
-                    cuda_check(cudaMemcpyAsync(thr_discard->p, upload(thr.data(), thr.size() * 8),
-                                               size_t(nsec) * 8, cudaMemcpyDeviceToDevice, ctx().stream),
-                               "cudaMemcpyAsync(thresholds)");
-                }
+                const double *dskip = static_cast<const double *>(upload(skip2.data(), skip2.size() * 8));
+                fp64_sweeps(1, thr64->p, dskip);
+                const double *dthr = static_cast<const double *>(upload(thr2.data(), thr2.size() * 8));
+                fp64_sweeps(max_sweeps, dthr, nullptr);
             }
-            fp64_sweeps(max_sweeps, thr_discard ? thr_discard->p : (thr64 ? thr64->p : nullptr));
             fw = w1->p;
             fr = vbuf->p;
         }

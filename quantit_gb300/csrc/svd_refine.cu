@@ -25,11 +25,13 @@ namespace qtt {
 namespace {
 
 // C[M x N] (column-major, ldc) = op(A) B', A = M x K (a_trans: stored K x M), and
-// B' = B (K x N) or, with b_ns, 1.5 I - 0.5 B (the Newton-Schulz factor).
+// B' = B (K x N) or, with b_ns, 1.5 I - 0.5 B (the Newton-Schulz factor).  sym bit 0: C is
+// symmetric (A^T A), only tiles on or above the diagonal are computed; bit 1: B is such a
+// matrix, its elements below the diagonal are read from above it.
 struct SecGemm {
     int64_t a_off, b_off, c_off;
     int32_t M, N, K, lda, ldb, ldc;
-    int32_t a_trans, b_ns, tile_start, pad;
+    int32_t a_trans, b_ns, tile_start, sym;
 };
 
 template <class TA, class TB>
@@ -49,6 +51,7 @@ __global__ void __launch_bounds__(256) k_secgemm(const TA *__restrict__ A, const
     const int tm = (d.M + 63) / 64;
     const int t = int(blockIdx.x) - d.tile_start;
     const int r0 = (t % tm) * 64, c0 = (t / tm) * 64;
+    if ((d.sym & 1) && c0 + 63 < r0) return;  // strictly below the diagonal of a symmetric C
     const TA *a = A + d.a_off;
     const TB *b = B + d.b_off;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -78,7 +81,8 @@ __global__ void __launch_bounds__(256) k_secgemm(const TA *__restrict__ A, const
             const int c = c0 + jj, kq = k0 + kb;
             double bv = 0.0;
             if (c < d.N && kq < d.K) {
-                bv = double(b[int64_t(c) * d.ldb + kq]);
+                const int lo = (d.sym & 2) ? min(kq, c) : kq, hi = (d.sym & 2) ? max(kq, c) : c;
+                bv = double(b[int64_t(hi) * d.ldb + lo]);
                 if (d.b_ns) bv = (kq == c ? 1.5 : 0.0) - 0.5 * bv;
             }
             Bs[kb][jj] = bv;
@@ -129,24 +133,29 @@ void secgemm(const TA *A, const TB *B, double *C, std::vector<SecGemm> &tasks, c
 }
 
 // Squared column norms of every sector matrix (one warp per column).
-__global__ void k_col_norms(const double *__restrict__ W, const SectorDesc *__restrict__ secs,
+template <class T>
+__global__ void k_col_norms(const T *__restrict__ W, const SectorDesc *__restrict__ secs,
                             double *__restrict__ out) {
     const SectorDesc sd = secs[blockIdx.y];
     const int lane = threadIdx.x & 31;
     const int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (col >= sd.q) return;
-    const double *w = W + sd.w_off + int64_t(col) * sd.p;
+    const T *w = W + sd.w_off + int64_t(col) * sd.p;
     double acc = 0.0;
-    for (int r = lane; r < sd.p; r += 32) acc = fma(w[r], w[r], acc);
+    for (int r = lane; r < sd.p; r += 32) acc = fma(double(w[r]), double(w[r]), acc);
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) out[sd.s_off + col] = acc;
 }
 
 }  // namespace
 
-void launch_col_norms(const double *W, const SectorDesc *secs, int nsec, int max_q, double *out) {
+void launch_col_norms(const void *W, const SectorDesc *secs, int nsec, int max_q, double *out, int f32) {
     if (nsec <= 0 || max_q <= 0) return;
-    k_col_norms<<<dim3(unsigned((max_q + 7) / 8), unsigned(nsec)), 256, 0, ctx().stream>>>(W, secs, out);
+    const dim3 grid(unsigned((max_q + 7) / 8), unsigned(nsec));
+    if (f32)
+        k_col_norms<float><<<grid, 256, 0, ctx().stream>>>(static_cast<const float *>(W), secs, out);
+    else
+        k_col_norms<double><<<grid, 256, 0, ctx().stream>>>(static_cast<const double *>(W), secs, out);
     count_launch();
     cuda_check(cudaGetLastError(), "column norm launch");
 }
@@ -157,13 +166,13 @@ void launch_svd_refine(const float *rot32, const double *w64, double *w1, double
     auto gram = [&]() {
         std::vector<SecGemm> t;
         for (const SectorDesc &s : secs)
-            t.push_back({s.rot_off, s.rot_off, s.rot_off, s.q, s.q, s.q, s.q, s.q, s.q, 1, 0, 0, 0});
+            t.push_back({s.rot_off, s.rot_off, s.rot_off, s.q, s.q, s.q, s.q, s.q, s.q, 1, 0, 0, 1});
         return t;
     };
     auto ns = [&]() {
         std::vector<SecGemm> t;
         for (const SectorDesc &s : secs)
-            t.push_back({s.rot_off, s.rot_off, s.rot_off, s.q, s.q, s.q, s.q, s.q, s.q, 0, 1, 0, 0});
+            t.push_back({s.rot_off, s.rot_off, s.rot_off, s.q, s.q, s.q, s.q, s.q, s.q, 0, 1, 0, 2});
         return t;
     };
     // Newton-Schulz step 1 from the FP32 rotation: G = V0^T V0, va = V0 (1.5 I - 0.5 G)
