@@ -87,16 +87,19 @@ def parse():
     p.add_argument("--svd-sweeps", type=int, default=3, help="svd workload: mixed sweeps before the theta is taken")
     p.add_argument("--save-state", default=None, help="svd workload: write the theta (block-list file)")
     p.add_argument("--state-file", default=None, help="svd workload: read the theta instead of sweeping")
-    p.add_argument("--serving-requests", type=int, default=16)
-    p.add_argument("--serving-rate", type=float, default=4.0,
-                   help="Poisson arrival rate (requests/s); above the service capacity the stream measures the "
-                        "saturated throughput and its queueing latency")
+    p.add_argument("--serving-requests", type=int, default=None,
+                   help="requests of the serving stream (default: 240 for --workload serving, 0 otherwise)")
+    p.add_argument("--serving-rate", type=float, default=0.0,
+                   help="Poisson arrival rate (requests/s); <= 0: --serving-load x the capacity measured on a "
+                        "burst first")
+    p.add_argument("--serving-load", type=float, default=0.7, help="offered load of the automatic rate")
+    p.add_argument("--serving-calibrate", type=int, default=48, help="requests of the capacity burst")
     p.add_argument("--serving-slots", type=int, default=8)
     p.add_argument("--serving-lanczos", type=int, default=4,
                    help="Lanczos steps per bond in the serving solves (1: QuantiT's one-step update)")
-    p.add_argument("--serving-fp64-every", type=int, default=4,
+    p.add_argument("--serving-fp64-every", type=int, default=8,
                    help="serial FP64 baseline on every k-th request of the stream")
-    p.add_argument("--serving-fp64-budget", type=float, default=300.0,
+    p.add_argument("--serving-fp64-budget", type=float, default=420.0,
                    help="stop the serial FP64 sample once this many seconds are spent")
     p.add_argument("--jacobi", default="block", choices=["block", "scalar"],
                    help="sector-SVD Jacobi kernel (block-cyclic where it fits, or scalar)")
@@ -350,30 +353,51 @@ def e2e_sweep(q, mpo, mps, args):
             "h2d_bytes_per_step": int(np.mean(h2d)), "d2h_bytes_per_step": int(np.mean(d2h)), "E": E}
 
 
-SERVING_REDUCED = dict(lengths=(16, 32, 64), bonds=(32, 64, 128, 256))
 SERVING_FULL = dict(lengths=(16, 32, 64, 128), bonds=(32, 64, 128, 256, 512))
 
 
-def serving_section(q, args, full):
-    """Continuous-batching solves of a seeded Poisson stream of XXZ requests (mixed
-    precision, converged to 1e-8 relative energy), and serial plain-FP64 solves of
-    every k-th request of the same stream as the baseline."""
+def serving_section(q, args, n_requests):
+    """Continuous-batching solves of a seeded Poisson stream of XXZ requests (L from
+    {16, 32, 64, 128}, D from {32, ..., 512}, delta from [0, 2]; mixed precision,
+    converged to 1e-8 relative energy).  With --serving-rate <= 0 the arrival rate is
+    --serving-load times the capacity measured first on a burst of
+    --serving-calibrate requests released at once (another seed), so the stream runs
+    below saturation and its latency is service, not queueing.  Every k-th request of
+    the stream is then solved alone in plain FP64 (serial, one at a time) for the
+    baseline throughput and the per-request |dE| per site and truncated weight."""
     from quantit_gb300 import serving
-    dist = SERVING_FULL if full else SERVING_REDUCED
-    reqs = serving.poisson_requests(args.serving_requests, rate=args.serving_rate, seed=0, **dist)
+    dist = SERVING_FULL
     mixed = args.mode if args.mode != "f64" else "tf32x3"
-    eng = serving.ServingEngine(slots=args.serving_slots, gemm=mixed,
-                                convergence=1e-8, max_sweeps=40, lanczos_steps=args.serving_lanczos)
+
+    def engine():
+        return serving.ServingEngine(slots=args.serving_slots, gemm=mixed, convergence=1e-8, max_sweeps=40,
+                                     lanczos_steps=args.serving_lanczos)
+    out = {"distribution": {"L": list(dist["lengths"]), "D": list(dist["bonds"]), "delta": [0.0, 2.0]},
+           "slots": args.serving_slots, "gemm": mixed, "lanczos_steps": args.serving_lanczos, "convergence": 1e-8}
+    rate = args.serving_rate
+    if rate <= 0:
+        burst = serving.poisson_requests(args.serving_calibrate, rate=0.0, seed=1, **dist)
+        eng = engine()
+        res = eng.run(burst, realtime=False)
+        cap = len(res) / max(r.done for r in res)
+        rate = args.serving_load * cap
+        out["capacity"] = {"requests": len(res), "solves_per_s": cap,
+                           "how": "burst released at once (seed 1); solves / time to the last completion"}
+    reqs = serving.poisson_requests(n_requests, rate=rate, seed=0, **dist)
+    eng = engine()
     res = eng.run(reqs, realtime=True)
     mk = max(r.done for r in res) - min(r.arrival for r in res)
-    out = serving.summarize([r.latency for r in res], mk, len(res))
-    out.update({"requests": len(reqs), "rate_per_s": args.serving_rate, "slots": args.serving_slots,
-                "distribution": {"L": list(dist["lengths"]), "D": list(dist["bonds"]), "delta": [0.0, 2.0]},
-                "convergence": 1e-8, "gemm": mixed, "lanczos_steps": args.serving_lanczos,
+    out.update(serving.summarize([r.latency for r in res], mk, len(res)))
+    lat = np.array([r.latency for r in res])
+    tw = np.array([r.truncated_weight for r in res], dtype=float)
+    out.update({"requests": len(reqs), "rate_per_s": rate, "p90_s": float(np.percentile(lat, 90)),
+                "offered_load": rate / out["capacity"]["solves_per_s"] if "capacity" in out else None,
                 "peak_concurrency": eng.peak_concurrency,
                 "memory_budget_bytes": eng.memory_budget, "peak_admitted_bytes": eng.peak_memory,
                 "errors": sum(1 for r in res if r.error),
                 "mean_service_s": float(np.mean([r.service for r in res])),
+                "mean_wait_s": float(np.mean([r.admitted - r.arrival for r in res])),
+                "truncated_weight": {"max": float(np.nanmax(tw)), "median": float(np.nanmedian(tw))},
                 "latency": "completion minus arrival (queueing included)"})
     sample, st = [], []
     t0 = time.perf_counter()
@@ -384,14 +408,20 @@ def serving_section(q, args, full):
                                          lanczos_steps=args.serving_lanczos)
         sample.append(r)
     svc = [x[0] for x in st]
-    mixed = {r.rid: r for r in res}
-    dE = [abs(mixed[r.rid].energy - x[1]) / r.L for r, x in zip(sample, st)]
+    byid = {r.rid: r for r in res}
+    dE = np.array([abs(byid[r.rid].energy - x[1]) / r.L for r, x in zip(sample, st)])
+    tw64 = np.array([x[3] for x in st], dtype=float)
+    twm = np.array([byid[r.rid].truncated_weight for r in sample], dtype=float)
     out["serial_fp64"] = {"sample": len(sample), "of_every": args.serving_fp64_every,
-                          "sampled": [[r.L, r.D] for r in sample],
+                          "sampled_L_D": [[r.L, r.D] for r in sample],
                           "solves_per_s": len(sample) / sum(svc), "mean_service_s": float(np.mean(svc)),
-                          "max_dE_per_site_vs_mixed": float(max(dE)),
-                          "note": "one solve at a time on the GPU, plain FP64"}
-    out["throughput_vs_serial_fp64"] = out["solves_per_s"] / out["serial_fp64"]["solves_per_s"]
+                          "dE_per_site": {"max": float(dE.max()), "median": float(np.median(dE))},
+                          "truncated_weight": {"max": float(np.nanmax(tw64)), "median": float(np.nanmedian(tw64))},
+                          "truncated_weight_mixed_same_requests": {"max": float(np.nanmax(twm)),
+                                                                   "median": float(np.nanmedian(twm))},
+                          "note": "one solve at a time on the GPU, plain FP64, same requests and seeds"}
+    base = out["capacity"]["solves_per_s"] if "capacity" in out else out["solves_per_s"]
+    out["capacity_vs_serial_fp64"] = base / out["serial_fp64"]["solves_per_s"]
     return out
 
 
@@ -840,11 +870,92 @@ def cylinder_main(args, rank, world, local):
             line["cpu_baseline"] = {"error": repr(e)}
         finally:
             shutil.rmtree(d, ignore_errors=True)
+    if rank == 0 and args.serving_requests:
+        try:
+            line["serving"] = serving_section(q, args, args.serving_requests)
+        except Exception as e:  # reported, never hidden
+            line["serving"] = {"error": repr(e)}
     tune = q.autotune_report().splitlines()
     line["autotune_classes"] = len(tune)
     if rank == 0:
         print("autotune:\n  " + "\n  ".join(tune), file=sys.stderr)
-        print(json.dumps(line))
+        print("full line: " + json.dumps(line), file=sys.stderr)
+        print(json.dumps(slim_cylinder_line(line)))
+
+
+def sig(x, n=4):
+    """x with floats rounded to n significant digits (recursively)."""
+    if isinstance(x, float):
+        return float(f"{x:.{n}g}") if np.isfinite(x) else x
+    if isinstance(x, dict):
+        return {k: sig(v, n) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [sig(v, n) for v in x]
+    return x
+
+
+def slim_cylinder_line(line):
+    """The printed line: every key of the contract, the comparison with FP64, the
+    roofline objects and the serving summary, with floats at 4 significant digits
+    (energies at 12) and without the per-sweep lists and notes, so the line stays
+    under 3 KB; the full line goes to stderr."""
+    keep = ("kernel", "bound", "achieved", "peak", "unit", "frac", "traffic", "per_launch_ms")
+    out = {k: line[k] for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                                "higher_is_better", "scaling", "vs_baseline", "dtype", "data")}
+    cfg = line["config"]
+    out["config"] = {"workload": cfg["workload"], "L": cfg["L"], "D": cfg["D"], "cutoff": cfg["cutoff"],
+                     "mpo": "compressed to bond dim 20", "update": "one-step Lanczos",
+                     "l2": "working set >> L2", "parallelism": cfg["parallelism"], "mode": cfg.get("mode")}
+    out["gpu_launches"] = line["gpu_launches"]
+    out["clocks"] = {k: line["clocks"].get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")}
+    for k in ("roofline", "roofline_gemm"):
+        if isinstance(line.get(k), dict):
+            out[k] = sig({a: b for a, b in line[k].items() if a in keep})
+    if isinstance(line.get("roofline_f64"), dict):
+        out["roofline_f64"] = {k: sig({a: b for a, b in v.items() if a in ("achieved", "unit", "frac")})
+                               for k, v in line["roofline_f64"].items()}
+    for k in ("kernel_time_ms", "kernel_time_ms_f64"):
+        if k in line:
+            out[k] = {a: round(b) for a, b in line[k].items()}
+    out["sweep_times_s"] = sig(line["sweeps"]["times_s"])
+    v = line.get("vs_fp64")
+    if isinstance(v, dict):
+        out["vs_fp64"] = dict(sig({k: v[k] for k in ("fp64_s_per_sweep", "mixed_s_per_sweep", "speedup_vs_fp64",
+                                                    "dE_per_site", "sweeps")}),
+                              E_fp64=sig(v["E_fp64"], 12), E_mixed=sig(v["E_mixed"], 12),
+                              trunc_fp64=sig(max(v["truncated_weight_fp64"])),
+                              trunc_mixed=sig(max(v["truncated_weight_mixed"])))
+    st = line.get("state", {})
+    if st:
+        out["state"] = {"ramp": [[r["D"], r["sweeps"], sig(r["s"], 3)] for r in st.get("ramp", [])],
+                        "prep_s": st.get("prep_wall_s")}
+    e = line.get("e2e")
+    if isinstance(e, dict):
+        out["e2e"] = sig({k: e[k] for k in ("value", "unit", "steps", "h2d_bytes_per_step", "d2h_bytes_per_step")
+                          if k in e})
+    c = line.get("cpu_baseline")
+    if isinstance(c, dict):
+        out["cpu_baseline"] = sig({k: c[k] for k in ("value", "unit", "cores", "kind", "sample", "error") if k in c})
+        if "sample" in out["cpu_baseline"]:
+            out["cpu_baseline"]["sample"] = out["cpu_baseline"]["sample"][:150]
+    sv = line.get("serving")
+    if isinstance(sv, dict):
+        out["serving"] = slim_serving(sv)
+    return out
+
+
+def slim_serving(sv):
+    if "error" in sv:
+        return sv
+    f = sv.get("serial_fp64", {})
+    return sig({"requests": sv["requests"], "rate_per_s": sv["rate_per_s"], "offered_load": sv.get("offered_load"),
+                "solves_per_s": sv["solves_per_s"], "p50_s": sv["p50_s"], "p99_s": sv["p99_s"],
+                "capacity_solves_per_s": sv.get("capacity", {}).get("solves_per_s"),
+                "trunc_max": sv["truncated_weight"]["max"], "errors": sv["errors"],
+                "fp64_serial_solves_per_s": f.get("solves_per_s"), "fp64_sample": f.get("sample"),
+                "dE_per_site_max": f.get("dE_per_site", {}).get("max"),
+                "trunc_fp64_max": f.get("truncated_weight", {}).get("max"),
+                "capacity_vs_serial_fp64": sv.get("capacity_vs_serial_fp64")})
 
 
 def main():
@@ -927,7 +1038,7 @@ def main():
             dist.destroy_process_group()
         return
     if args.workload == "serving":
-        sv = serving_section(q, args, full=True)
+        sv = serving_section(q, args, args.serving_requests if args.serving_requests is not None else 240)
         if rank == 0:
             print(json.dumps({"metric": "solves/s (XXZ ground states, Poisson arrivals) at p99 latency",
                               "value": sv["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": 1,
@@ -1008,9 +1119,9 @@ def main():
                                               f"x {s.factor:.1f} size-weighted bonds per sweep"}
         except Exception as e:  # reported, never hidden
             line["cpu_baseline"] = {"error": repr(e)}
-    if rank == 0 and args.serving_requests > 0 and not hub:
+    if rank == 0 and args.serving_requests and not hub:
         try:
-            line["serving"] = serving_section(q, args, full=False)
+            line["serving"] = serving_section(q, args, args.serving_requests)
         except Exception as e:  # reported, never hidden
             line["serving"] = {"error": repr(e)}
     if rank == 0:

@@ -81,6 +81,18 @@ int qtt_autotune_report(char *buf, int64_t cap, int64_t *len);
  * norm as its value, far below any value a truncation keeps; the FP64 sweeps of the
  * mixed path resolve what its FP32 sweeps dropped. */
 int qtt_set_svd_deflation(int on);
+/* Block-sparsity planner of tensordot / tensorgdot (the charge check and merge-join of
+ * sources/btensor.cpp:783-883,1998-2110): mode 0 plans on the host, 1 on the device
+ * wherever the device planner's limits allow (at most 16384 blocks per operand, keys
+ * within 63 bits, at least one contracted leg), 2 on the device for contractions with
+ * at least auto_blocks blocks in the two operands together (default: mode 2, 512).
+ * Both emit the same output block list and pair order, bit for bit.  Inside CUDA-graph
+ * capture the host plans. */
+int qtt_set_planner(int mode, int64_t auto_blocks);
+/* Planner calls since the last reset: calls[0] on the host, calls[1] on the device,
+ * calls[2] device attempts beyond its limits (planned on the host); secs[0], secs[1]:
+ * host wall seconds spent planning on each path.  reset != 0 clears them. */
+int qtt_planner_stats(int64_t *calls, double *secs, int reset);
 /* Persistent split-TF32 / split-BF16 GEMMs (one CTA per SM walking the tile list, double-buffered TMEM
  * accumulator) for launches of at least two tiles per SM; on by default (no reference
  * counterpart). */

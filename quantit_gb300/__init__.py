@@ -32,6 +32,29 @@ def set_svd_deflation(on):
     call("qtt_set_svd_deflation", 1 if on else 0)
 
 
+def set_planner(mode="auto", auto_blocks=512):
+    """Block-sparsity planner of tensordot: "host", "device" (wherever the device
+    planner's limits allow) or "auto" (device for contractions of at least
+    ``auto_blocks`` blocks in both operands together; the default)."""
+    from ._lib import call
+    modes = {"host": 0, "device": 1, "auto": 2}
+    if mode not in modes:
+        raise ValueError(f"planner mode must be one of {sorted(modes)}")
+    call("qtt_set_planner", modes[mode], int(auto_blocks))
+
+
+def planner_stats(reset=False):
+    """{"host_calls", "device_calls", "device_fallbacks", "host_s", "device_s"}: planner
+    calls and the host wall seconds spent planning on each path."""
+    import ctypes as C
+    from ._lib import call
+    calls = (C.c_int64 * 3)()
+    secs = (C.c_double * 2)()
+    call("qtt_planner_stats", calls, secs, 1 if reset else 0)
+    return {"host_calls": calls[0], "device_calls": calls[1], "device_fallbacks": calls[2], "host_s": secs[0],
+            "device_s": secs[1]}
+
+
 def set_persistent_gemm(on):
     """Persistent split-TF32 GEMM for launches of many tiles (on by default)."""
     from ._lib import call

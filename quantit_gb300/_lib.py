@@ -38,6 +38,8 @@ SIGNATURES = {
     "qtt_set_jacobi_kernel": (C.c_int, [C.c_int]),
     "qtt_set_autotune": (C.c_int, [C.c_int]),
     "qtt_set_svd_deflation": (C.c_int, [C.c_int]),
+    "qtt_set_planner": (C.c_int, [C.c_int, i64]),
+    "qtt_planner_stats": (C.c_int, [P(i64), P(C.c_double), C.c_int]),
     "qtt_set_persistent_gemm": (C.c_int, [C.c_int]),
     "qtt_autotune_report": (C.c_int, [C.c_char_p, i64, P(i64)]),
     "qtt_device_memory": (C.c_int, [P(i64), P(i64)]),

@@ -99,6 +99,15 @@ int qtt_set_autotune(int on) {
 int qtt_set_svd_deflation(int on) {
     return guarded([&] { qtt::set_svd_deflation(on); });
 }
+int qtt_set_planner(int mode, int64_t auto_blocks) {
+    return guarded([&] { qtt::set_planner(mode, auto_blocks); });
+}
+int qtt_planner_stats(int64_t *calls, double *secs, int reset) {
+    return guarded([&] {
+        if (!calls || !secs) qtt::fail(qtt::ERR_INVALID_ARGUMENT, "null output pointer");
+        qtt::planner_stats(calls, secs, reset != 0);
+    });
+}
 int qtt_set_persistent_gemm(int on) {
     return guarded([&] { qtt::set_persistent_gemm(on); });
 }

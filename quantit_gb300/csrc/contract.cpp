@@ -9,6 +9,7 @@
 // grouped GEMM launch.  Operands whose natural row-major layout already is the
 // (free x contracted) or (contracted x free) matrix are read in place (plain or
 // transposed access); only a genuinely scattered leg order is packed first.
+#include <chrono>
 #include <numeric>
 
 #include "contract.h"
@@ -77,8 +78,31 @@ bool is_identity(const std::vector<int64_t> &p) {
 }
 }  // namespace
 
+namespace {
+void host_join(ContractPlan &P, const BT &A, const BT &B, int dl);
+void set_operand_modes(ContractPlan &P);
+
+bool device_present() {
+    static const bool present = [] {
+        int n = 0;
+        return cudaGetDeviceCount(&n) == cudaSuccess && n > 0;
+    }();
+    return present;
+}
+
+[[noreturn]] void fail_sections(const ContractPlan &P, int i, bool size) {
+    const std::string a = std::to_string(P.dA[i]), b = std::to_string(P.dB[i]);
+    if (size)
+        fail(ERR_CHECK, "contracted section sizes differ between dim " + a + " of the left tensor and dim " + b +
+                            " of the right tensor");
+    fail(ERR_CHECK, "contracted conserved numbers need to sum to zero, but there is a violation when contracting dim " +
+                        a + " of the left tensor with dim " + b + " of the right tensor");
+}
+}  // namespace
+
 ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_t> &dA_in,
                               const std::vector<int64_t> &dB_in) {
+    const auto t_start = std::chrono::steady_clock::now();
     // compute_tdot_shape / check_product_compat (btensor.cpp:783-883)
     if (dA_in.size() != dB_in.size()) fail(ERR_CHECK, "both dimension lists should have the same length.");
     if (!(A.g == B.g)) fail(ERR_CHECK, "the two tensors have different type of conserved quantities");
@@ -87,22 +111,29 @@ ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_
     P.dB = norm_dims(dB_in, B.rank);
     const int dl = int(P.dA.size());
     auto adA = A.addrs(), adB = B.addrs();
-    for (int i = 0; i < dl; ++i) {
-        int64_t a = P.dA[i], b = P.dB[i];
-        if (A.sbd[a] != B.sbd[b])
-            fail(ERR_CHECK, "contracted dimensions need to match, but first has " + std::to_string(A.sbd[a]) +
-                                " sections along dim " + std::to_string(a) + "  and second has " +
-                                std::to_string(B.sbd[b]) + " sections along dim " + std::to_string(b));
-        for (int64_t s = 0; s < A.sbd[a]; ++s) {
-            if (!qeq(qadd(A.cv[adA[a] + s], B.cv[adB[b] + s], A.g), Charge{}, A.g))
-                fail(ERR_CHECK, "contracted conserved numbers need to sum to zero, but there is a violation when "
-                                "contracting dim " + std::to_string(a) + " of the left tensor with dim " +
-                                    std::to_string(b) + " of the right tensor");
-            if (A.ssz[adA[a] + s] != B.ssz[adB[b] + s])
-                fail(ERR_CHECK, "contracted section sizes differ between dim " + std::to_string(a) +
-                                    " of the left tensor and dim " + std::to_string(b) + " of the right tensor");
+    // dimension by dimension: the section count, then every section's charges and size
+    auto host_check = [&]() {
+        for (int i = 0; i < dl; ++i) {
+            int64_t a = P.dA[i], b = P.dB[i];
+            if (A.sbd[a] != B.sbd[b])
+                fail(ERR_CHECK, "contracted dimensions need to match, but first has " + std::to_string(A.sbd[a]) +
+                                    " sections along dim " + std::to_string(a) + "  and second has " +
+                                    std::to_string(B.sbd[b]) + " sections along dim " + std::to_string(b));
+            for (int64_t s = 0; s < A.sbd[a]; ++s) {
+                if (!qeq(qadd(A.cv[adA[a] + s], B.cv[adB[b] + s], A.g), Charge{}, A.g)) fail_sections(P, i, false);
+                if (A.ssz[adA[a] + s] != B.ssz[adB[b] + s]) fail_sections(P, i, true);
+            }
         }
-    }
+    };
+    bool counts_match = true;
+    for (int i = 0; i < dl; ++i) counts_match = counts_match && A.sbd[P.dA[i]] == B.sbd[P.dB[i]];
+    const int mode = planner_mode();
+    const int64_t nbl = A.nblocks() + B.nblocks();
+    // the device planner checks the section charges itself; graph capture (no
+    // synchronisation allowed) and machines without a device plan on the host
+    const bool want_dev = mode != 0 && dl > 0 && counts_match && A.nblocks() > 0 && B.nblocks() > 0 &&
+                          (mode == 1 || nbl >= planner_auto_blocks()) && device_present() && !ctx().capturing;
+    if (!want_dev) host_check();
     std::vector<char> cA(A.rank, 0), cB(B.rank, 0);
     for (auto d : P.dA) cA[d] = 1;
     for (auto d : P.dB) cB[d] = 1;
@@ -138,13 +169,36 @@ ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_
             o.cv.push_back(B.cv[adB[d] + s]);
         }
     }
+    int on_device = 0;
+    if (want_dev) {
+        int bad_dim = 0;
+        bool bad_size = false;
+        on_device = plan_join_device(P, A, B, &bad_dim, &bad_size);
+        if (on_device < 0) fail_sections(P, bad_dim, bad_size);
+        if (!on_device) {
+            planner_account(2, 0.0);
+            host_check();
+        }
+    }
+    if (!on_device) host_join(P, A, B, dl);
+    o.boff.assign(P.out_p0.size(), 0);
+    o.compact_offsets();
+    set_operand_modes(P);
+    planner_account(on_device ? 1 : 0,
+                    std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count());
+    return P;
+}
+
+namespace {
+void host_join(ContractPlan &P, const BT &A, const BT &B, int dl) {
+    BT &o = P.out;
     // merge-join (btensor.cpp:1998-2114): for every run of A (equal free prefix) and
     // every run of B, in that nested order, the pairs with equal contracted suffix.
     // Only the runs of B that share a suffix with the run of A can produce pairs, so
     // they are found through a sorted (suffix, run) index of B instead of trying
     // every run pair: the same output block list and pair order, in
     // O(n log n + pairs) instead of O(runs_A x runs_B).
-    Keyed t1 = permuted_sorted(A, p1), t2 = permuted_sorted(B, p2p);
+    Keyed t1 = permuted_sorted(A, P.p1), t2 = permuted_sorted(B, P.p2p);
     const int nfa = A.rank - dl, nfb = B.rank - dl;
     auto r1 = runs(t1, nfa, dl == 0), r2 = runs(t2, nfb, dl == 0);
     auto join = [&](const std::pair<size_t, size_t> &ra, const std::pair<size_t, size_t> &rb) {
@@ -199,9 +253,11 @@ ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_
             for (int32_t rb : cand) join(ra, r2[rb]);
         }
     }
-    o.boff.assign(P.out_p0.size(), 0);
-    o.compact_offsets();
+}
+
+void set_operand_modes(ContractPlan &P) {
     // operand layouts
+    const std::vector<int64_t> &p1 = P.p1, &p2 = P.p2;
     P.a_mode = is_identity(p1) ? 0 : -1;
     if (P.a_mode < 0) {
         // rotation: contracted legs leading in dims order, free legs trailing in order
@@ -215,8 +271,8 @@ ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_
         rot.insert(rot.end(), P.dB.begin(), P.dB.end());
         P.b_mode = is_identity(rot) ? 1 : 2;
     }
-    return P;
 }
+}  // namespace
 
 namespace {
 // permuted copy of every block of t with permutation perm (compact, block-list order)

@@ -19,6 +19,13 @@ struct ContractPlan {
     int b_mode = 0;  // 0: B block is (contracted x free) row-major, 1: stored transposed, 2: packed
 };
 
+// The merge-join on the device (planner.cu): fills the pair tables and the output
+// block list of P, whose legs, permutations and output sections are set.  Returns 1
+// when done, 0 when the inputs exceed the device planner's limits (nothing filled),
+// -1 when a contracted section pair fails the charge (or, with *bad_size, the size)
+// check, at contracted dimension *bad_dim.
+int plan_join_device(ContractPlan &P, const BT &A, const BT &B, int *bad_dim, bool *bad_size);
+
 ContractPlan plan_contraction(const BT &A, const BT &B, const std::vector<int64_t> &dA,
                               const std::vector<int64_t> &dB);
 // Run the grouped GEMM of a plan into out (whose offsets index out's buffer).

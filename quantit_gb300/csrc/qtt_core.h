@@ -22,6 +22,12 @@
 
 namespace qtt {
 
+#ifdef __CUDACC__
+#define QTT_HD __host__ __device__
+#else
+#define QTT_HD
+#endif
+
 constexpr int MAXC = 4;     // group factors per charge (U(1)xU(1)xZ(n)... up to 4)
 constexpr int MAXRANK = 8;  // largest tensor rank handled by the kernels
 
@@ -105,7 +111,7 @@ struct Charge {
     int16_t v[MAXC] = {0, 0, 0, 0};
 };
 
-inline Charge qadd(const Charge &a, const Charge &b, const Group &g) {
+QTT_HD inline Charge qadd(const Charge &a, const Charge &b, const Group &g) {
     Charge r;
     for (int i = 0; i < g.n; ++i) {
         if (g.mod[i]) {
@@ -130,7 +136,7 @@ inline Charge qinv(const Charge &a, const Group &g) {
     }
     return r;
 }
-inline bool qeq(const Charge &a, const Charge &b, const Group &g) {
+QTT_HD inline bool qeq(const Charge &a, const Charge &b, const Group &g) {
     for (int i = 0; i < g.n; ++i)
         if (a.v[i] != b.v[i]) return false;
     return true;
@@ -375,7 +381,17 @@ std::string autotune_report();
 // Persistent tensor-core GEMM for launches of at least two tiles per SM (on by default).
 void set_persistent_gemm(int on);
 int persistent_gemm();
-// Deflation of numerically zero columns in the FP32 SVD of a truncating svd (off by default).
+// Block-sparsity planner of tensordot: 0 host merge-join, 1 device (planner.cu)
+// wherever its limits allow, 2 device for contractions of at least
+// planner_auto_blocks() blocks in the two operands together (the default).
+void set_planner(int mode, int64_t auto_blocks);
+int planner_mode();
+int64_t planner_auto_blocks();
+// planner calls and host wall seconds (planning only): [0] host calls, [1] device
+// calls, [2] device attempts that fell back to the host; secs[0] host, secs[1] device
+void planner_stats(int64_t *calls, double *secs, bool reset);
+void planner_account(int which, double secs);
+// Deflation of numerically zero columns in the sector SVDs of a truncating svd (on by default).
 void set_svd_deflation(int on);
 int svd_deflation();
 // Non-zero when a tensor-core kernel gave up on a bounded wait since the last

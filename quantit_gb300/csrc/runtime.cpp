@@ -212,6 +212,36 @@ int persistent_gemm() { return g_persistent_gemm; }
 void set_svd_deflation(int on) { g_svd_deflation = on ? 1 : 0; }
 int svd_deflation() { return g_svd_deflation; }
 
+namespace {
+std::atomic<int> g_planner{2};
+std::atomic<int64_t> g_planner_auto{512};
+std::mutex g_plan_mu;
+int64_t g_plan_calls[3] = {0, 0, 0};
+double g_plan_secs[2] = {0.0, 0.0};
+}  // namespace
+void set_planner(int mode, int64_t auto_blocks) {
+    if (mode < 0 || mode > 2) fail(ERR_INVALID_ARGUMENT, "planner mode must be 0 (host), 1 (device) or 2 (auto)");
+    if (auto_blocks < 0) fail(ERR_INVALID_ARGUMENT, "the automatic planner threshold must be >= 0");
+    g_planner = mode;
+    g_planner_auto = auto_blocks;
+}
+int planner_mode() { return g_planner; }
+int64_t planner_auto_blocks() { return g_planner_auto; }
+void planner_account(int which, double secs) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    g_plan_calls[which] += 1;
+    if (which < 2) g_plan_secs[which] += secs;
+}
+void planner_stats(int64_t *calls, double *secs, bool reset) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    for (int i = 0; i < 3; ++i) calls[i] = g_plan_calls[i];
+    for (int i = 0; i < 2; ++i) secs[i] = g_plan_secs[i];
+    if (reset) {
+        for (auto &c : g_plan_calls) c = 0;
+        for (auto &x : g_plan_secs) x = 0.0;
+    }
+}
+
 // ---------------------------------------------------------------- btensor helpers
 std::string check_tensor(const BT &t) {
     std::ostringstream M;

@@ -37,13 +37,14 @@ class SolveRequest:
 
 
 class SolveResult:
-    __slots__ = ("rid", "L", "delta", "D", "energy", "sweeps", "arrival", "admitted", "started", "done", "footprint",
-                 "error")
+    __slots__ = ("rid", "L", "delta", "D", "energy", "sweeps", "truncated_weight", "arrival", "admitted", "started",
+                 "done", "footprint", "error")
 
     def __init__(self, req, footprint):
         self.rid, self.L, self.delta, self.D = req.rid, req.L, req.delta, req.D
         self.energy = math.nan
         self.sweeps = 0
+        self.truncated_weight = math.nan
         self.arrival = req.arrival
         self.admitted = self.started = self.done = math.nan
         self.footprint = footprint
@@ -113,7 +114,8 @@ def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, che
     leave the FP64 range on long chains), run two-site DMRG to the relative energy
     convergence (``lanczos_steps``-step Lanczos per bond, matvecs replayed from CUDA
     graphs), write the optimised MPS to ``checkpoint_dir`` when given, return
-    (E, sweeps)."""
+    (E, sweeps, truncated weight): the truncated weight is the largest relative
+    discarded weight sum(dropped s^2) / sum(s^2) over the bonds of the last sweep."""
     from . import serialize
     mpo = networks.xxz(req.L, req.delta)
     if getattr(req, "resume", None):
@@ -132,7 +134,7 @@ def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, che
     if checkpoint_dir:
         import os
         serialize.save(os.path.join(checkpoint_dir, f"request_{req.rid}.npz"), mps)
-    return E, len(log.energies)
+    return E, len(log.energies), (log.truncated_weights[-1] if log.truncated_weights else 0.0)
 
 
 class ServingEngine:
@@ -148,7 +150,7 @@ class ServingEngine:
                                lanczos_steps=lanczos_steps)
         if checkpoint_dir:
             self.solve_args["checkpoint_dir"] = checkpoint_dir
-        # solver(req, **solve_args) -> (E, sweeps); the default is the GPU solve
+        # solver(req, **solve_args) -> (E, sweeps[, truncated weight]); the default is the GPU solve
         self.solver = solver or solve
         self.footprint = footprint or (lambda r: footprint_bytes(r.L, r.D))
         self.on_device = solver is None
@@ -185,7 +187,10 @@ class ServingEngine:
                 req, res = item
                 res.started = time.perf_counter() - t0
                 try:
-                    res.energy, res.sweeps = self.solver(req, **self.solve_args)
+                    out = self.solver(req, **self.solve_args)
+                    res.energy, res.sweeps = out[0], out[1]
+                    if len(out) > 2:
+                        res.truncated_weight = out[2]
                 except Exception as e:  # reported per request, the server keeps going
                     res.error = f"{type(e).__name__}: {e}"
                 res.done = time.perf_counter() - t0
@@ -237,12 +242,13 @@ class ServingEngine:
 
 
 def serial_solve_times(requests, **solve_args):
-    """Service time of every request solved alone, one after another, on the calling thread."""
+    """(service time, E, sweeps, truncated weight) of every request solved alone, one
+    after another, on the calling thread."""
     out = []
     for r in requests:
         t = time.perf_counter()
-        E, sw = solve(r, **solve_args)
-        out.append((time.perf_counter() - t, E, sw))
+        E, sw, tw = solve(r, **solve_args)
+        out.append((time.perf_counter() - t, E, sw, tw))
     return out
 
 

@@ -89,3 +89,48 @@ def test_environments_match_the_oracle():
             for (k, x), (_, y) in zip(dev.blocks(), ora.blocks):
                 np.testing.assert_allclose(x, y, rtol=1e-11, atol=1e-13)
     del env
+
+
+def _ed_ground_energy(L, couplings):
+    """Lowest eigenvalue of sum J S_i.S_j in the Sz=0 sector (sparse Lanczos)."""
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    states = np.array([s for s in range(1 << L) if bin(s).count("1") == L // 2], dtype=np.int64)
+    index = {int(s): k for k, s in enumerate(states)}
+    rows, cols, vals = [], [], []
+    diag = np.zeros(len(states))
+    for i, j, J in couplings:
+        bi = (states >> (L - 1 - i)) & 1
+        bj = (states >> (L - 1 - j)) & 1
+        diag += J * np.where(bi == bj, 0.25, -0.25)
+        flip = states ^ ((1 << (L - 1 - i)) | (1 << (L - 1 - j)))
+        for k in np.nonzero(bi != bj)[0]:
+            rows.append(index[int(flip[k])])
+            cols.append(k)
+            vals.append(0.5 * J)
+    n = len(states)
+    H = sp.csr_matrix((vals, (rows, cols)), shape=(n, n)) + sp.diags(diag)
+    return float(spl.eigsh(H, k=1, which="SA")[0][0])
+
+
+@pytest.mark.parametrize("compress", [False, True])
+def test_cylinder_dmrg_energy_is_the_state_energy_and_exact(compress):
+    """4 x 4 snake cylinder at a bond dimension that holds the ground state exactly
+    (256 = 2^8): the Ritz energy the sweep reports (k-step and one-step Lanczos) equals
+    the FP64 <psi|H|psi>/<psi|psi> of the state the sweep leaves, and both the exact
+    ground energy, with the automaton MPO and with the compressed one."""
+    Lx, Ly = 4, 4
+    mpo = NET.cylinder_heisenberg(Lx, Ly, 1.0, "snake", compress=compress)
+    L = len(mpo)
+    E_ed = _ed_ground_energy(L, NET.cylinder_couplings(Lx, Ly, 1.0, "snake"))
+    mps = NET.random_bMPS(32, mpo, q.conserved.Z(0), seed=3)
+    mps.move_oc(0)
+    mps.normalize_center()
+    for D, steps, sweeps in ((32, 4, 2), (256, 4, 4), (256, 1, 2)):
+        log = q.algorithms.dmrg_log_sweeptime()
+        q.algorithms.dmrg(mpo, mps, q.algorithms.dmrg_options(
+            cutoff=1e-14, convergence_criterion=0.0, max_bond=D, min_bond=1, maximum_iterations=sweeps,
+            lanczos_steps=steps, final_energy_fp64=False), log)
+        e, n2 = q.algorithms.mps_energy(mpo, mps)
+        assert log.energies[-1] == pytest.approx(e / n2, rel=1e-9, abs=1e-9), (D, steps, log.energies, e / n2)
+    assert e / n2 == pytest.approx(E_ed, rel=1e-9, abs=1e-9)

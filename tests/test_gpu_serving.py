@@ -20,11 +20,12 @@ def test_results_same_alone_and_in_the_mix():
     eng = serving.ServingEngine(slots=4, gemm="tf32x3", convergence=1e-8, max_sweeps=30)
     mixed = eng.run(REQS, realtime=False)
     assert eng.peak_concurrency >= 2
-    for (t, E, sw), r in zip(alone, mixed):
+    for (t, E, sw, tw), r in zip(alone, mixed):
         assert r.error is None, r.error
         # per-stream kernels are deterministic: the mix changes timing, not arithmetic
         assert r.energy == pytest.approx(E, rel=1e-12, abs=1e-12), (r.rid, r.energy, E)
         assert r.sweeps == sw
+        assert r.truncated_weight == tw
     qq.set_autotune(True)
 
 
@@ -33,5 +34,5 @@ def test_mixed_serving_energies_match_fp64_solves():
     ref = serving.serial_solve_times(sub, gemm="f64", convergence=1e-10, max_sweeps=30)
     eng = serving.ServingEngine(slots=4, gemm="tf32x3", convergence=1e-8, max_sweeps=30)
     res = eng.run(sub, realtime=False)
-    for (t, E, sw), r in zip(ref, res):
+    for (t, E, sw, tw), r in zip(ref, res):
         assert abs(r.energy - E) / r.L < 1e-7, (r.rid, r.energy, E)

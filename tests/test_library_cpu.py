@@ -233,7 +233,7 @@ def test_reshape_as_acceptance_matches_oracle(mods):
 
 def test_tuning_switches_and_dmrg_options_round_trip():
     """The tuning switches with no reference counterpart (persistent GEMM, SVD deflation,
-    autotuner, Jacobi kernel) are plain host settings: they take effect without a GPU, and
+    autotuner, Jacobi kernel, planner) are plain host settings: they take effect without a GPU, and
     dmrg_options carries the build's extra fields into the C struct unchanged."""
     import quantit_gb300 as q
     for on in (False, True):
@@ -245,6 +245,17 @@ def test_tuning_switches_and_dmrg_options_round_trip():
         q.set_jacobi_kernel(kernel)
     with pytest.raises(ValueError):
         q.set_jacobi_kernel(7)
+    # the planner switch: every mode is accepted without a GPU (with no device the
+    # host plans), unknown modes and negative thresholds are refused
+    for mode in ("host", "device", "auto"):
+        q.set_planner(mode, 512)
+    with pytest.raises(ValueError):
+        q.set_planner("gpu")
+    with pytest.raises(ValueError):
+        q.set_planner("auto", -1)
+    q.set_planner("auto", 512)   # the default
+    st = q.planner_stats(reset=True)
+    assert set(st) == {"host_calls", "device_calls", "device_fallbacks", "host_s", "device_s"}
     o = q.algorithms.dmrg_options(gemm="bf16x3", lanczos_steps=4, cuda_graphs=False, svd_warm_start=False,
                                   final_energy_fp64=False)._c()
     assert (o.gemm_mode, o.lanczos_steps, o.cuda_graphs, o.svd_warm_start, o.final_energy_fp64) == (2, 4, 0, 0, 0)
