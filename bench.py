@@ -101,6 +101,8 @@ def parse():
                    help="serial FP64 baseline on every k-th request of the stream")
     p.add_argument("--serving-fp64-budget", type=float, default=420.0,
                    help="stop the serial FP64 sample once this many seconds are spent")
+    p.add_argument("--planner", default="auto", choices=["host", "device", "auto"],
+                   help="block-sparsity planner of the contractions (auto: device for >= 512 blocks)")
     p.add_argument("--jacobi", default="block", choices=["block", "scalar"],
                    help="sector-SVD Jacobi kernel (block-cyclic where it fits, or scalar)")
     return p.parse_args()
@@ -806,10 +808,12 @@ def cylinder_main(args, rank, world, local):
     torch.cuda.synchronize()
     launches0 = q.stats.launches()
     log = state_log(q, keep_after=args.compare_sweeps)
+    q.planner_stats(reset=True)
     sampler.start()
     t_mix, _, S_mix = sweeps_call(q, mpo, S0, args.steps, args.mode, args.D, log)
     torch.cuda.synchronize()
     clocks = sampler.stop()
+    plan_st = q.planner_stats(reset=True)
     launches = q.stats.launches() - launches0
     kinds = {k: q.stats.get(k) for k in q.stats.KINDS}
     q.stats.enable(False)
@@ -818,7 +822,7 @@ def cylinder_main(args, rank, world, local):
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": f"{args.mode}+f64svd+f64" if args.mode != "f64" else "f64",
             "data": "synthetic", "config": dict(cfg, mode=args.mode), "gpu_launches": int(launches),
-            "clocks": clocks}
+            "clocks": clocks, "planner": dict(plan_st, mode=args.planner)}
     P = peaks()
     pc = {}
     dom = max((k for k in kinds if k != "svd_fp64"), key=lambda k: kinds[k]["ms"])
@@ -994,6 +998,7 @@ def main():
         import quantit_gb300 as q
         q.ensure_init(local)
         q.set_jacobi_kernel(args.jacobi)
+        q.set_planner(args.planner)
         if args.svd_deflation is not None:
             q.set_svd_deflation(bool(args.svd_deflation))
         cylinder_main(args, rank, world, local)
@@ -1028,6 +1033,7 @@ def main():
     import quantit_gb300 as q
     q.ensure_init(local)
     q.set_jacobi_kernel(args.jacobi)
+    q.set_planner(args.planner)
     if args.svd_deflation is not None:
         q.set_svd_deflation(bool(args.svd_deflation))
     if args.workload in ("contraction", "svd"):
@@ -1061,12 +1067,14 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     launches0 = q.stats.launches()
+    q.planner_stats(reset=True)
     sampler.start()
     t0 = time.perf_counter()
     Es, ts, mps2 = run_sweeps(q, mpo, mps1, args.steps, args.mode, args.D)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
+    plan_st = q.planner_stats(reset=True)
     launches = q.stats.launches() - launches0
     kinds = {k: q.stats.get(k) for k in q.stats.KINDS}
     q.stats.enable(False)
@@ -1098,7 +1106,9 @@ def main():
             "sweep_times_s": ts, "wall_s": wall, "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()},
             "roofline": roofline(dom, kinds[dom], P, args.mode, pc),
             "roofline_gemm": roofline("gemm", kinds["gemm"], P, args.mode, pc),
-            "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e}
+            "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e,
+            "planner": dict(plan_st, mode=args.planner, note="calls and host wall seconds of the contraction "
+                                                             "planner over the timed sweeps")}
     if cmp:
         line["vs_fp64"] = cmp
     # the autotuner's decisions go to stderr: one line each would push the metric keys

@@ -123,13 +123,28 @@ class btensor:
         _lib.call("qtt_bt_blocks", self._h, idx, None)
         return [tuple(idx[b * r:(b + 1) * r]) for b in range(nb)]
 
-    def block_shape(self, idx):
-        sbd, ssz, _, _ = self.structure()
+    def _sizes(self):
+        """(sections_by_dim, section_sizes) without the charges."""
+        r, ns, nc, nb, nnz, dt, hd = self._meta()
+        sbd = (C.c_int64 * max(r, 1))()
+        ssz = (C.c_int64 * max(ns, 1))()
+        cv = (C.c_int16 * max(ns * nc, 1))()
+        sel = (C.c_int16 * max(nc, 1))()
+        mods = (C.c_uint16 * max(nc, 1))()
+        _lib.call("qtt_bt_structure", self._h, sbd, ssz, cv, sel, mods)
+        return list(sbd[:r]), list(ssz[:ns])
+
+    @staticmethod
+    def _shape_of(sizes, idx):
+        sbd, ssz = sizes
         shp, a = [], 0
         for d, i in enumerate(idx):
             shp.append(ssz[a + i])
             a += sbd[d]
         return tuple(shp)
+
+    def block_shape(self, idx):
+        return self._shape_of(self._sizes(), idx)
 
     def has_data(self):
         return bool(self._meta()[6])
@@ -147,11 +162,12 @@ class btensor:
         flat = np.empty(max(nnz, 1), dtype=npdt)
         if nnz:
             _lib.call("qtt_bt_download", self._h, flat.ctypes.data_as(C.c_void_p), flat.nbytes)
+        sizes = self._sizes()
         out, o = [], 0
         for b in range(nb):
             key = tuple(idx[b * r:(b + 1) * r])
             n = numel[b]
-            out.append((key, flat[o:o + n].reshape(self.block_shape(key)).copy()))
+            out.append((key, flat[o:o + n].reshape(self._shape_of(sizes, key)).copy()))
             o += n
         return out
 
@@ -170,16 +186,17 @@ class btensor:
     # ------------------------------------------------------------- construction
     def set_blocks(self, blocks):
         """Replace the block list with [(index, array)] (uploads to the device)."""
-        r = self.dim()
+        sizes = self._sizes()
+        dt = self.dtype
         idx, arrs = [], []
         for k, v in blocks:
             idx.extend(int(i) for i in k)
-            shp = self.block_shape(tuple(k))
-            a = np.ascontiguousarray(v, dtype=self.dtype)
+            shp = self._shape_of(sizes, tuple(k))
+            a = np.ascontiguousarray(v, dtype=dt)
             if a.shape != shp:
                 raise ValueError(f"block {tuple(k)} has shape {a.shape}, {shp} expected")
             arrs.append(a.ravel())
-        data = np.concatenate(arrs) if arrs else np.zeros(1, dtype=self.dtype)
+        data = np.concatenate(arrs) if arrs else np.zeros(1, dtype=dt)
         _lib.call("qtt_bt_set_blocks", self._h, len(arrs), _lib.i64_array(idx),
                   data.ctypes.data_as(C.c_void_p))
         return self
