@@ -322,13 +322,43 @@ def roofline(kind, st, P, mode, peaks_cache):
             import torch
             peaks_cache[key] = matmul_peak_tflops(torch.float32 if fp32 else torch.float64)
         ach = st["work"] / sec / 1e12
-        return dict(base, bound="latency (grid barrier per block-Jacobi step, CTA barrier per round)" if kind == "svd" else "fp64",
+        return dict(base, bound="latency (block-Jacobi barriers)" if kind == "svd" else "fp64",
                     achieved=ach, peak=peaks_cache[key], unit="TFLOP/s", frac=ach / peaks_cache[key],
                     peak_source=f"cuBLAS {'SGEMM' if fp32 else 'DGEMM'} measured in this run")
     ach = st["work"] / sec / 1e9
     peak = P.get("hbm_gbs", 6800.0)
     return dict(base, bound="hbm", achieved=ach, peak=peak, unit="GB/s", frac=ach / peak,
                 peak_source="MEASURED_PEAKS.json hbm_gbs (of measured)")
+
+
+WORK_ONLY = ("jacobi_fp32", "jacobi_fp64")   # statistics kinds that carry FLOPs but no time
+
+
+def timed_kinds(kinds):
+    return {k: v for k, v in kinds.items() if k not in WORK_ONLY}
+
+
+def svd_stages(kinds, mode, peaks_cache):
+    """The sector SVDs by precision stage: each stage's time and the FLOPs its Jacobi
+    sweeps performed (sweeps x (6 p q^2 + 3 q^3) per sector; the FP64 stage of the mixed
+    path adds its Newton-Schulz and W V products), against the SGEMM / DGEMM measured in
+    this run.  The algorithmic count of the roofline object does not depend on the method;
+    these figures show how busy each stage keeps its pipe."""
+    import torch
+    out = {}
+    t_all, t64 = kinds["svd"]["ms"], kinds["svd_fp64"]["ms"]
+    stages = [("fp32_stage", t_all - t64, kinds["jacobi_fp32"]["work"], "fp32"),
+              ("fp64_stage", t64, kinds["jacobi_fp64"]["work"], "fp64")] if mode != "f64" else \
+        [("fp64_stage", t_all, kinds["jacobi_fp64"]["work"], "fp64")]
+    for name, ms, work, key in stages:
+        if ms <= 0:
+            continue
+        if key not in peaks_cache:
+            peaks_cache[key] = matmul_peak_tflops(torch.float32 if key == "fp32" else torch.float64)
+        tf = work / (ms / 1e3) / 1e12
+        out[name] = {"ms": ms, "jacobi_tflops": tf, "peak": peaks_cache[key],
+                     "frac": tf / peaks_cache[key], "peak_source": f"cuBLAS {'SGEMM' if key == 'fp32' else 'DGEMM'}"}
+    return out
 
 
 def e2e_sweep(q, mpo, mps, args):
@@ -482,7 +512,7 @@ def svd_workload(q, args):
     t = float(np.mean(ts))
     return {"metric": "s per truncated sector SVD of a mid-chain DMRG theta", "value": t, "unit": "s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.mode != "f64" else "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.mode != "f64" else "f64",
             "data": "synthetic", "config": {"workload": f"svd(theta, 2, 1e-10, 1, {args.D}) of the middle theta "
                                                         f"of a D={args.D} DMRG state of the "
                                                         + ("6x12 cylinder" if args.model == "cylinder"
@@ -491,8 +521,9 @@ def svd_workload(q, args):
                                             "l2": "flushed between steps (256 MB write)"},
             "jacobi_sweeps_per_sector": sweeps, "fp32_sweeps_per_sector": fp32_sweeps,
             "kept": int(sum(d.section_sizes)),
-            "roofline": roofline("svd", kinds["svd"], peaks(), args.mode, {}),
-            "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()}}
+            "roofline": dict(roofline("svd", kinds["svd"], peaks(), args.mode, {}),
+                             stages=svd_stages(kinds, args.mode, {})),
+            "kernel_time_ms": {k: v["ms"] for k, v in timed_kinds(kinds).items()}}
 
 
 def contraction_workload(q, args):
@@ -555,7 +586,7 @@ def contraction_workload(q, args):
             "accuracy": {"C_rel_err": (num / den) ** 0.5, "d_max_rel_err": float(np.max(np.abs(m["d"][:nk] - f["d"][:nk])) / f["d"][0]),
                          "kept_mixed": m["kept"], "kept_fp64": f["kept"]},
             "roofline_gemm": roofline("gemm", m["kinds"]["gemm"], P, args.mode, {}),
-            "kernel_time_ms": {k: v["ms"] for k, v in m["kinds"].items()}}
+            "kernel_time_ms": {k: v["ms"] for k, v in timed_kinds(m["kinds"]).items()}}
 
 
 # --------------------------------------------------------------------------- cylinder
@@ -825,10 +856,12 @@ def cylinder_main(args, rank, world, local):
             "clocks": clocks, "planner": dict(plan_st, mode=args.planner)}
     P = peaks()
     pc = {}
-    dom = max((k for k in kinds if k != "svd_fp64"), key=lambda k: kinds[k]["ms"])
+    dom = max((k for k in timed_kinds(kinds) if k != "svd_fp64"), key=lambda k: kinds[k]["ms"])
     line["roofline"] = roofline(dom, kinds[dom], P, args.mode, pc)
+    if dom == "svd":
+        line["roofline"]["stages"] = svd_stages(kinds, args.mode, pc)
     line["roofline_gemm"] = roofline("gemm", kinds["gemm"], P, args.mode, pc)
-    line["kernel_time_ms"] = {k: round(v["ms"], 1) for k, v in kinds.items()}
+    line["kernel_time_ms"] = {k: round(v["ms"], 1) for k, v in timed_kinds(kinds).items()}
     line["sweeps"] = {"times_s": [round(x, 3) for x in log.time_list], "middle_bond": log.bond_list,
                       "truncated_weight": log.truncated_weights, "ritz_E": log.energies}
     # the same state in FP64: compare_sweeps sweeps, against the first as many timed mixed sweeps
@@ -842,7 +875,9 @@ def cylinder_main(args, rank, world, local):
         q.stats.enable(False)
         # the plain path against its own roofline: FP64 GEMMs and FP64 Jacobi against cuBLAS DGEMM
         line["roofline_f64"] = {k: roofline(k, k64[k], P, "f64", pc) for k in ("gemm", "svd")}
-        line["kernel_time_ms_f64"] = {k: round(v["ms"], 1) for k, v in k64.items()}
+        if line["roofline_f64"]["svd"]:
+            line["roofline_f64"]["svd"]["stages"] = svd_stages(k64, "f64", pc)
+        line["kernel_time_ms_f64"] = {k: round(v["ms"], 1) for k, v in timed_kinds(k64).items()}
         t64 = lf.time_list[1:] if len(lf.time_list) > 1 else lf.time_list
         tm = log.time_list[1:] if len(log.time_list) > 1 else log.time_list
         Sm = log.kept if log.kept is not None else S_mix
@@ -912,12 +947,19 @@ def slim_cylinder_line(line):
                      "l2": "working set >> L2", "parallelism": cfg["parallelism"], "mode": cfg.get("mode")}
     out["gpu_launches"] = line["gpu_launches"]
     out["clocks"] = {k: line["clocks"].get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")}
+    def stages(r):  # {stage: [ms, Jacobi TFLOP/s, fraction of the stage's cuBLAS peak]}
+        return {n.split("_")[0]: sig([v["ms"], v["jacobi_tflops"], v["frac"]]) for n, v in r["stages"].items()}
     for k in ("roofline", "roofline_gemm"):
         if isinstance(line.get(k), dict):
             out[k] = sig({a: b for a, b in line[k].items() if a in keep})
+            if line[k].get("stages"):
+                out[k]["stages"] = stages(line[k])
     if isinstance(line.get("roofline_f64"), dict):
         out["roofline_f64"] = {k: sig({a: b for a, b in v.items() if a in ("achieved", "unit", "frac")})
-                               for k, v in line["roofline_f64"].items()}
+                               for k, v in line["roofline_f64"].items() if v}
+        sv = line["roofline_f64"].get("svd")
+        if sv and sv.get("stages"):
+            out["roofline_f64"]["svd"]["stages"] = stages(sv)
     for k in ("kernel_time_ms", "kernel_time_ms_f64"):
         if k in line:
             out[k] = {a: round(b) for a, b in line[k].items()}
@@ -1097,13 +1139,14 @@ def main():
     e2e = e2e_sweep(q, mpo, mps1, args)
     P = peaks()
     pc = {}
-    dom = max((k for k in kinds if k != "svd_fp64"), key=lambda k: kinds[k]["ms"])
+    dom = max((k for k in timed_kinds(kinds) if k != "svd_fp64"), key=lambda k: kinds[k]["ms"])
     line = {"metric": METRIC, "value": job_per_sweep, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.mode == "f64" else f"{args.mode}+f64svd+f64",
             "data": "synthetic", "config": dict(cfg, mode=args.mode, jacobi=args.jacobi), "ritz_energies": Es,
             "energy_fp64": E_mixed, "energy_per_site": E_mixed / args.L, "fp64_energy_eval_s": t_eval,
-            "sweep_times_s": ts, "wall_s": wall, "kernel_time_ms": {k: v["ms"] for k, v in kinds.items()},
+            "sweep_times_s": ts, "wall_s": wall,
+            "kernel_time_ms": {k: v["ms"] for k, v in timed_kinds(kinds).items()},
             "roofline": roofline(dom, kinds[dom], P, args.mode, pc),
             "roofline_gemm": roofline("gemm", kinds["gemm"], P, args.mode, pc),
             "gpu_launches": int(launches), "clocks": clocks, "e2e": e2e,

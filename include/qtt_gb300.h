@@ -297,7 +297,9 @@ int qtt_svd_dense_noalloc(const double *a, int64_t m, int64_t n, double *u, doub
  * algorithmic work: kind 0 block GEMM (FLOP), 1 permute (bytes), 2 sector SVD
  * (FLOP, LAPACK-class count 4p^2q + 8pq^2 + 9q^3 per p x q sector), 3 elementwise (bytes),
  * 4 sector pack (bytes), 5 the FP64 stage of the mixed path's sector SVDs (time only; part
- * of kind 2). */
+ * of kind 2), 6 / 7 the FLOPs the sector SVDs' Jacobi sweeps performed in FP32 / FP64
+ * (work only: sweeps x (6 p q^2 + 3 q^3) per p x q sector, plus 8 q^3 + 2 p q^2 for the
+ * mixed path's FP64 refinement products). */
 int qtt_stats_enable(int on);
 int qtt_stats_reset(void);
 int qtt_stats_get(int kind, double *ms, double *work, int64_t *launches);

@@ -81,7 +81,8 @@ def set_jacobi_kernel(which):
 
 class stats:
     """Per-kernel-class device time (CUDA events) and algorithmic work."""
-    KINDS = {"gemm": 0, "permute": 1, "svd": 2, "elementwise": 3, "pack": 4, "svd_fp64": 5}
+    KINDS = {"gemm": 0, "permute": 1, "svd": 2, "elementwise": 3, "pack": 4, "svd_fp64": 5, "jacobi_fp32": 6,
+             "jacobi_fp64": 7}
 
     @staticmethod
     def enable(on=True):

@@ -459,6 +459,36 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             fr = vbuf->p;
         }
         last_sweeps() = {f32 ? ibuf64 : ibuf, ibuf, nsec, f32 != 0};
+        if (mode == 0 && stats_enabled() && !ctx().capturing) {
+            // the sweeps' FLOPs, read from the sweep counters once the statistics are read
+            cudaEvent_t raw = nullptr;
+            cuda_check(cudaEventCreateWithFlags(&raw, cudaEventDisableTiming), "cudaEventCreate");
+            cuda_check(cudaEventRecord(raw, ctx().stream), "cudaEventRecord");
+            auto ev = std::shared_ptr<CUevent_st>(raw, [](cudaEvent_t e) { cudaEventDestroy(e); });
+            std::vector<std::pair<double, double>> pq;
+            for (const SectorDesc &d : D.desc) pq.push_back({double(d.p), double(d.q)});
+            auto flops = [ev, pq, nsec](const BufPtr &b, int extra, bool refine) {
+                cudaEventSynchronize(ev.get());
+                std::vector<int> sw(size_t(std::max(nsec, 1)), 0);
+                cudaMemcpy(sw.data(), b->p, size_t(nsec) * sizeof(int), cudaMemcpyDeviceToHost);
+                double f = 0.0;
+                for (int i = 0; i < nsec; ++i) {
+                    const double P = pq[i].first, Q = pq[i].second;
+                    f += double(sw[i] + extra) * (6.0 * P * Q * Q + 3.0 * Q * Q * Q);
+                    if (refine) f += 8.0 * Q * Q * Q + 2.0 * P * Q * Q;
+                }
+                return f;
+            };
+            if (f32) {
+                BufPtr b32 = ibuf, b64 = ibuf64;
+                const int extra = discard.empty() ? 0 : 1;
+                stats_defer_work(ST_JAC32, [flops, b32] { return flops(b32, 0, false); });
+                stats_defer_work(ST_JAC64, [flops, b64, extra] { return flops(b64, extra, true); });
+            } else {
+                BufPtr b = ibuf;
+                stats_defer_work(ST_JAC64, [flops, b] { return flops(b, 0, false); });
+            }
+        }
         BufPtr permbuf;
         int64_t max_elems = 0;
         if (cap == 0) {

@@ -404,8 +404,22 @@ inline void tc_error_raise() {
 // ---------------------------------------------------------------- timing statistics
 // Per-kernel-class device time measured with CUDA events on the launching stream,
 // plus the algorithmic work each launch did (FLOPs or bytes).
-// ST_SVD64: the FP64 stage of the mixed path's sector SVDs (a part of ST_SVD's time)
-enum StatKind : int { ST_GEMM = 0, ST_PERMUTE = 1, ST_SVD = 2, ST_ELEMWISE = 3, ST_PACK = 4, ST_SVD64 = 5, ST_COUNT = 6 };
+// ST_SVD64: the FP64 stage of the mixed path's sector SVDs (a part of ST_SVD's time).
+// ST_JAC32 / ST_JAC64: work only (no time): the FLOPs the sector SVDs' Jacobi sweeps
+// performed in FP32 and in FP64 (sweeps x (6 p q^2 + 3 q^3) per p x q sector, the
+// one-sided Jacobi count; the FP64 count adds the mixed path's Newton-Schulz and W V
+// products, 8 q^3 + 2 p q^2).
+enum StatKind : int {
+    ST_GEMM = 0,
+    ST_PERMUTE = 1,
+    ST_SVD = 2,
+    ST_ELEMWISE = 3,
+    ST_PACK = 4,
+    ST_SVD64 = 5,
+    ST_JAC32 = 6,
+    ST_JAC64 = 7,
+    ST_COUNT = 8
+};
 void stats_enable(bool on);
 bool stats_enabled();
 // Work known only after the kernels ran (e.g. Jacobi sweeps): resolved when read.
