@@ -166,9 +166,20 @@ struct JacobiParams {
     int *rotated;  // nsec * max_sweeps flags, zero on entry: a rotation happened in (sector, sweep)
     const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
     T *dnorm;      // per column (s_off + column): squared norm when deflated, 0 otherwise
-    const T *skip; // per sector (null: none): a pair whose squared norms are both below it is
-                   // left as it is (both columns lie below what the caller keeps)
+    const T *skip; // per sector (null: none): squared discard level of pair_skipped
 };
+
+// Pairs the decoupling FP64 sweep of a truncating mixed-precision SVD leaves alone
+// (skip = the squared discard level of the sector, 0: none): both columns below it, or
+// the smaller one below it and under 2^-14 of the larger in norm.  After the FP32 sweeps
+// a pair's coupling is at most a few 1e-6 of the product of its norms, so rotating the
+// second kind would move the larger (kept) column by under 1e-14 of its norm; the
+// smaller column is discarded by the truncation anyway.
+template <class T>
+__device__ __forceinline__ bool pair_skipped(T al, T be, T skip) {
+    const T lo = al < be ? al : be, hi = al < be ? be : al;
+    return lo < skip && (hi < skip || lo < T(3.7252902984619140625e-09) * hi);  // 2^-28 in squared norms
+}
 
 // Rotation of one column pair by one warp.  With R > 0 (p <= 32 R) every lane
 // first loads its R elements of both columns into registers -- one round trip to
@@ -219,7 +230,7 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
         }
         return true;
     }
-    if (al < skip && be < skip) return false;
+    if (pair_skipped(al, be, skip)) return false;
     if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
     T sn, tau;
     rot_params(al, be, ga, sn, tau);
@@ -390,8 +401,7 @@ struct BJacobiParams {
     int max_q;     // widest sector (columns)
     const T *defl; // per sector: squared-norm deflation threshold (null: no deflation)
     T *dnorm;      // per column (s_off + column): squared norm when deflated, 0 otherwise
-    const T *skip; // per sector (null: none): a pair whose squared norms are both below it is
-                   // left as it is (both columns lie below what the caller keeps)
+    const T *skip; // per sector (null: none): squared discard level of pair_skipped
 };
 
 __device__ __forceinline__ int bj_items(int q, int B) {
@@ -486,7 +496,7 @@ template <class T, int R>
 __device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T thr, T &sn, T &tau, T &dx,
                                           T &dy, T skip) {
     if (al == T(0) || be == T(0)) return false;
-    if (al < skip && be < skip) return false;
+    if (pair_skipped(al, be, skip)) return false;
     const T ga = bj_dot(x, y);
     if (ga == T(0)) return false;
     T t;

@@ -195,6 +195,63 @@ def test_mixed_truncated_svd_is_fp64_accurate(kernel, defl):
         np.testing.assert_allclose(R[k], a, atol=1e-12 * float(np.max(np.abs(a))), rtol=0)
 
 
+@pytest.mark.parametrize("kernel", ["block", "scalar"])
+def test_truncation_aware_fp64_stage_keeps_fp64_accuracy(kernel):
+    """A truncation to a quarter of the values (max_size), with every sector's spectrum
+    spread over 13 decades: the threshold lies far above FP32 resolution, so the mixed
+    path's FP64 stage leaves the columns below half its estimate out of the sweeps
+    (pairs of two of them, and pairs of one with a column over 2^14 times larger, in the
+    decoupling sweep; every pair of theirs afterwards).  The kept values match LAPACK to
+    1e-12 of the largest, the kept singular vectors match LAPACK's to 1e-10, the kept
+    factors are isometries to FP64 precision, and the plain FP64 path keeps the same."""
+    rng = np.random.default_rng(97)
+    shapes = [(160, 140), (120, 100), (90, 90), (40, 30)]
+    blocks, ref = [], []
+    for i, (m, n) in enumerate(shapes):
+        k = min(m, n)
+        sv = np.logspace(0, -13, k) * (0.5 + 0.5 * rng.uniform())
+        u, _ = np.linalg.qr(rng.standard_normal((m, k)))
+        v, _ = np.linalg.qr(rng.standard_normal((n, k)))
+        blocks.append(((i, i), (u * sv) @ v.T))
+        ref.append(np.linalg.svd(blocks[-1][1]))
+    legs = [[(m, Z(i)) for i, (m, _) in enumerate(shapes)], [(n, Z(-i)) for i, (_, n) in enumerate(shapes)]]
+    t = q.btensor(legs, Z(0))
+    t.set_blocks(blocks)
+    keep = sum(min(sh) for sh in shapes) // 4
+    pooled = np.sort(np.concatenate([r[1] for r in ref]))[::-1]
+    smax = pooled[0]
+    q.set_autotune(False)
+    q.set_jacobi_kernel(kernel)
+    try:
+        plain = q.linalg.svd(t, 1, 1e-14, min_size=1, max_size=keep)
+        q.set_gemm_mode("tf32x3")
+        U, d, V = q.linalg.svd(t, 1, 1e-14, min_size=1, max_size=keep)
+    finally:
+        q.set_jacobi_kernel("block")
+        q.set_gemm_mode("f64")
+        q.set_autotune(True)
+    assert sum(b.size for _, b in d.blocks()) == keep
+    assert plain[1].block_indices() == d.block_indices()
+    new_section = {k[0]: k[1] for k, _ in U.blocks()}
+    dv = dict(d.blocks())
+    Ub = dict(U.blocks())
+    for i, (uref, sref, _) in enumerate(ref):
+        if i not in new_section:
+            assert sref[0] <= pooled[keep - 1]
+            continue
+        got = dv[(new_section[i],)]
+        kk = len(got)
+        assert kk == int(np.sum(sref >= pooled[keep - 1]))
+        np.testing.assert_allclose(got, sref[:kk], atol=1e-12 * smax, rtol=0)
+        ug = Ub[(i, new_section[i])]
+        overlap = np.abs(np.sum(ug * uref[:, :kk], axis=0))
+        np.testing.assert_allclose(overlap, np.ones(kk), atol=1e-10, rtol=0)
+    for (k1, x), (k2, y) in zip(plain[1].blocks(), d.blocks()):
+        np.testing.assert_allclose(x, y, atol=1e-12 * smax, rtol=0)
+    assert _isometry_error(U) < 1e-11
+    assert _isometry_error(V) < 1e-11
+
+
 def test_truncated_svd_drops_exact_zero_values_like_the_oracle():
     """A truncation keeps only values strictly above its threshold less 2 eps, so an
     exact zero singular value is never kept, whatever min_size asks (the oracle's
