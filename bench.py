@@ -67,7 +67,9 @@ def parse():
     p.add_argument("--converge-sweeps", type=int, default=2,
                    help="cylinder: ramp-style sweeps at D before the warm-up (state preparation)")
     p.add_argument("--e2e-steps", type=int, default=2, help="cylinder: sweeps timed through the public API")
-    p.add_argument("--cpu-bonds", type=int, default=6, help="cylinder: bonds of the stratified CPU sample")
+    p.add_argument("--cpu-bonds", type=int, default=None,
+                   help="cylinder: bonds (strata) of the CPU sample, spread evenly over the chain (default: one "
+                        "per timed update, so that the timed updates visit every stratum once)")
     p.add_argument("--cpu-steps", type=int, default=3, help="cylinder: CPU bond updates in our arm's cpu_baseline")
     p.add_argument("--prepare-cpu-sample", default=None,
                    help="internal: build the timed state on the GPU and write it with the environments of "
@@ -75,6 +77,7 @@ def parse():
     p.add_argument("--cpu-sample", default=None,
                    help="internal: time oracle bond updates on the state written to this directory")
     p.add_argument("--cpu-threads", type=int, default=0, help="internal: BLAS threads of --cpu-sample (0: all)")
+    p.add_argument("--cpu-offset", type=int, default=0, help="internal: first stratum of --cpu-sample")
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--svd-deflation", type=int, default=None,
                    help="1/0: numerically null columns leave the sector-SVD sweeps of a truncating svd")
@@ -88,18 +91,18 @@ def parse():
     p.add_argument("--save-state", default=None, help="svd workload: write the theta (block-list file)")
     p.add_argument("--state-file", default=None, help="svd workload: read the theta instead of sweeping")
     p.add_argument("--serving-requests", type=int, default=None,
-                   help="requests of the serving stream (default: 240 for --workload serving, 0 otherwise)")
-    p.add_argument("--serving-rate", type=float, default=0.0,
-                   help="Poisson arrival rate (requests/s); <= 0: --serving-load x the capacity measured on a "
-                        "burst first")
+                   help="requests of the serving stream (default: 200 for --workload serving, 0 otherwise)")
+    p.add_argument("--serving-rate", type=float, default=0.25,
+                   help="Poisson arrival rate (requests/s), below the ~0.38 solves/s the full distribution "
+                        "saturates at; <= 0: --serving-load x the capacity measured on a burst first")
     p.add_argument("--serving-load", type=float, default=0.7, help="offered load of the automatic rate")
     p.add_argument("--serving-calibrate", type=int, default=48, help="requests of the capacity burst")
     p.add_argument("--serving-slots", type=int, default=8)
     p.add_argument("--serving-lanczos", type=int, default=4,
                    help="Lanczos steps per bond in the serving solves (1: QuantiT's one-step update)")
-    p.add_argument("--serving-fp64-every", type=int, default=8,
+    p.add_argument("--serving-fp64-every", type=int, default=10,
                    help="serial FP64 baseline on every k-th request of the stream")
-    p.add_argument("--serving-fp64-budget", type=float, default=420.0,
+    p.add_argument("--serving-fp64-budget", type=float, default=300.0,
                    help="stop the serial FP64 sample once this many seconds are spent")
     p.add_argument("--planner", default="auto", choices=["host", "device", "auto"],
                    help="block-sparsity planner of the contractions (auto: device for >= 512 blocks)")
@@ -422,6 +425,8 @@ def serving_section(q, args, n_requests):
     out.update(serving.summarize([r.latency for r in res], mk, len(res)))
     lat = np.array([r.latency for r in res])
     tw = np.array([r.truncated_weight for r in res], dtype=float)
+    print("serving stream: " + json.dumps(serving.summarize([r.latency for r in res], mk, len(res))),
+          file=sys.stderr, flush=True)
     out.update({"requests": len(reqs), "rate_per_s": rate, "p90_s": float(np.percentile(lat, 90)),
                 "offered_load": rate / out["capacity"]["solves_per_s"] if "capacity" in out else None,
                 "peak_concurrency": eng.peak_concurrency,
@@ -439,6 +444,7 @@ def serving_section(q, args, n_requests):
         st += serving.serial_solve_times([r], gemm="f64", convergence=1e-8, max_sweeps=40,
                                          lanczos_steps=args.serving_lanczos)
         sample.append(r)
+        print(f"serial fp64: request {r.rid} L={r.L} D={r.D} {st[-1][0]:.1f} s", file=sys.stderr, flush=True)
     svc = [x[0] for x in st]
     byid = {r.rid: r for r in res}
     dE = np.array([abs(byid[r.rid].energy - x[1]) / r.L for r, x in zip(sample, st)])
@@ -677,7 +683,7 @@ def write_cpu_sample(q, mpo, mps, outdir, nbonds, D):
     return bonds
 
 
-def cpu_sample(path, steps, threads):
+def cpu_sample(path, steps, threads, offset=0):
     """Oracle bond updates (dmrg_2sites_update: theta, one-step Lanczos, truncated sector
     SVD, environment update; sources/dmrg.cpp:145-207) on the saved state, cycling over
     the sampled bonds; returns the seconds of every update per bond."""
@@ -695,7 +701,7 @@ def cpu_sample(path, steps, threads):
     bonds = meta["bonds"]
     times = {b: [] for b in bonds}
     for k in range(steps):
-        b = bonds[k % len(bonds)]
+        b = bonds[(k + offset) % len(bonds)]
         mps = list(mps0)
         env = [None] * (L + 2)
         env[b], env[b + 3] = envs[b]
@@ -705,14 +711,16 @@ def cpu_sample(path, steps, threads):
     return {"bonds": bonds, "times": {str(b): v for b, v in times.items()}, "threads": threads, "L": L}
 
 
-def run_cpu_sample(path, steps, threads):
-    """cpu_sample in a child process with `threads` BLAS threads (0: the default, all cores)."""
+def run_cpu_sample(path, steps, threads, offset=0):
+    """cpu_sample in a child process with `threads` BLAS threads (0: the default, all cores),
+    starting at stratum `offset`."""
     env = dict(os.environ)
     if threads:
         for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
             env[k] = str(threads)
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-sample", path, "--cpu-steps",
-                        str(steps), "--cpu-threads", str(threads)], capture_output=True, text=True, env=env)
+                        str(steps), "--cpu-threads", str(threads), "--cpu-offset", str(offset)],
+                       capture_output=True, text=True, env=env)
     if r.returncode != 0:
         raise RuntimeError(f"CPU sample failed: {r.stderr.strip()[-400:]}")
     return json.loads(r.stdout.strip().splitlines()[-1])
@@ -762,7 +770,7 @@ def reference_arm_cylinder(args, cfg):
         cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--prepare-cpu-sample", d, "--D", str(args.D),
                "--warmup", str(args.warmup), "--ramp-sweeps", str(args.ramp_sweeps), "--ramp-lanczos",
                str(args.ramp_lanczos), "--converge-sweeps", str(args.converge_sweeps), "--cpu-bonds",
-               str(args.cpu_bonds), "--mode", args.mode, "--seed", str(args.seed)]
+               str(args.cpu_bonds or max(args.steps, 1)), "--mode", args.mode, "--seed", str(args.seed)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             return {"impl": "reference", "unavailable": "state preparation failed: " + r.stderr.strip()[-300:]}
@@ -777,8 +785,13 @@ def reference_arm_cylinder(args, cfg):
         for b, t in flat[args.warmup:]:
             timed[b].append(t)
         est, per = sweep_estimate({"times": timed, "L": smp["L"]})
-        one = run_cpu_sample(d, min(nb, 2), 1)
-        est1, _ = sweep_estimate(one)
+        # one BLAS thread: one update at the middle stratum, against all threads at that bond
+        mid = nb // 2
+        bmid = str(smp["bonds"][mid])
+        one = run_cpu_sample(d, 1, 1, offset=mid)
+        t1 = float(one["times"][bmid][0])
+        tall = float(np.mean(smp["times"][bmid]))
+        est1 = est * t1 / tall
     finally:
         shutil.rmtree(d, ignore_errors=True)
     host = cpu_host()
@@ -791,8 +804,9 @@ def reference_arm_cylinder(args, cfg):
             "data": "synthetic", "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": est, "unit": UNIT, "cores": host["nproc"], "kind": "port", "sample": sample,
                              "one_thread": {"value": est1, "unit": UNIT, "cores": 1,
-                                            "sample": f"{len(one['bonds'])} bond updates at 1 BLAS thread "
-                                                      f"(bonds {one['bonds'][:2]})"}},
+                                            "sample": f"bond {bmid}: {t1:.2f} s at 1 BLAS thread against "
+                                                      f"{tall:.2f} s at {host['nproc']}; the sweep estimate "
+                                                      f"scaled by that ratio"}},
             "per_stratum_s": per,
             "e2e": {"value": est, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -888,6 +902,7 @@ def cylinder_main(args, rank, world, local):
             "speedup_vs_fp64": float(np.mean(t64)) / float(np.mean(tm)),
             "dE_per_site": abs(Em - E64) / (CYL_LX * CYL_LY), "E_fp64": E64, "E_mixed": Em, "sweeps": n,
             "truncated_weight_fp64": lf.truncated_weights, "truncated_weight_mixed": log.truncated_weights[:n],
+            "ritz_E_fp64": lf.energies, "ritz_E_mixed": log.energies[:n],
             "note": "both from the timed state; per-sweep wall times of the sweeps after the first of each call; "
                     "energies are FP64 <psi|H|psi>/<psi|psi> after the same number of sweeps"}
     line["state"] = info
@@ -897,7 +912,7 @@ def cylinder_main(args, rank, world, local):
         import tempfile
         d = tempfile.mkdtemp(prefix="qtt_cpu_sample_")
         try:
-            write_cpu_sample(q, mpo, S0, d, args.cpu_bonds, args.D)
+            write_cpu_sample(q, mpo, S0, d, args.cpu_bonds or args.cpu_steps, args.D)
             smp = run_cpu_sample(d, args.cpu_steps, 0)
             est, per = sweep_estimate(smp)
             host = cpu_host()
@@ -1007,7 +1022,7 @@ def slim_serving(sv):
 def main():
     args = parse()
     if args.cpu_sample:
-        print(json.dumps(cpu_sample(args.cpu_sample, args.cpu_steps, args.cpu_threads)))
+        print(json.dumps(cpu_sample(args.cpu_sample, args.cpu_steps, args.cpu_threads, args.cpu_offset)))
         return
     if args.prepare_cpu_sample:
         import quantit_gb300 as q
@@ -1015,7 +1030,7 @@ def main():
         if args.D is None:
             args.D = 2048
         mpo, S0, _ = prepare_cylinder(q, args, args.seed)
-        write_cpu_sample(q, mpo, S0, args.prepare_cpu_sample, args.cpu_bonds, args.D)
+        write_cpu_sample(q, mpo, S0, args.prepare_cpu_sample, args.cpu_bonds or 6, args.D)
         return
     rank, world, local = dist_env()
     hub = args.model == "hubbard"
@@ -1086,7 +1101,7 @@ def main():
             dist.destroy_process_group()
         return
     if args.workload == "serving":
-        sv = serving_section(q, args, args.serving_requests if args.serving_requests is not None else 240)
+        sv = serving_section(q, args, args.serving_requests if args.serving_requests is not None else 200)
         if rank == 0:
             print(json.dumps({"metric": "solves/s (XXZ ground states, Poisson arrivals) at p99 latency",
                               "value": sv["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": 1,
