@@ -107,7 +107,14 @@ def device_memory():
     return f.value, t.value
 
 
-def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, checkpoint_dir=None, lanczos_steps=4):
+def ramp_stages(D, first=32):
+    """Bond dimensions a solve passes through: D/4 and D/2 where they are at least
+    ``first``, then D."""
+    return [d for d in (D // 4, D // 2) if d >= first] + [int(D)]
+
+
+def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, checkpoint_dir=None, lanczos_steps=4,
+          ramp=True, ramp_convergence=1e-6, ramp_sweeps=10):
     """One request on the calling thread: build the MPO and the seeded random MPS (or
     read the request's checkpoint), bring the MPS to canonical form (move_oc(0) and
     normalisation, in FP64: a raw random MPS's environments shrink like D^-i and
@@ -115,17 +122,33 @@ def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, che
     convergence (``lanczos_steps``-step Lanczos per bond, matvecs replayed from CUDA
     graphs), write the optimised MPS to ``checkpoint_dir`` when given, return
     (E, sweeps, truncated weight): the truncated weight is the largest relative
-    discarded weight sum(dropped s^2) / sum(s^2) over the bonds of the last sweep."""
+    discarded weight sum(dropped s^2) / sum(s^2) over the bonds of the last sweep.
+
+    With ``ramp`` a random start begins at the first of ``ramp_stages(D)`` and is swept
+    at each smaller bond dimension to ``ramp_convergence`` (at most ``ramp_sweeps``
+    sweeps) before the sweeps at D, which run to ``convergence`` as without it: most
+    sweeps then run at the cheaper bond dimensions.  The sweep count returned covers all
+    stages."""
     from . import serialize
     mpo = networks.xxz(req.L, req.delta)
+    stages = [req.D]
     if getattr(req, "resume", None):
         mps = serialize.load(req.resume)
         if len(mps) != req.L:
             raise ValueError("the checkpoint's length differs from the request's")
     else:
-        mps = networks.random_bmps(req.L, req.D, seed=req.seed)
+        if ramp:
+            stages = ramp_stages(req.D)
+        mps = networks.random_bmps(req.L, stages[0], seed=req.seed)
     mps.move_oc(0)
     mps.normalize_center()
+    sweeps = 0
+    for Dk in stages[:-1]:
+        log = algorithms.dmrg_log_sweeptime()
+        algorithms.dmrg(mpo, mps, algorithms.dmrg_options(
+            cutoff=cutoff, convergence_criterion=ramp_convergence, max_bond=Dk, min_bond=1,
+            maximum_iterations=ramp_sweeps, gemm=gemm, final_energy_fp64=True, lanczos_steps=lanczos_steps), log)
+        sweeps += len(log.energies)
     opts = algorithms.dmrg_options(cutoff=cutoff, convergence_criterion=convergence, max_bond=req.D, min_bond=1,
                                    maximum_iterations=max_sweeps, gemm=gemm, final_energy_fp64=True,
                                    lanczos_steps=lanczos_steps)
@@ -134,7 +157,7 @@ def solve(req, gemm="tf32x3", convergence=1e-8, max_sweeps=40, cutoff=1e-10, che
     if checkpoint_dir:
         import os
         serialize.save(os.path.join(checkpoint_dir, f"request_{req.rid}.npz"), mps)
-    return E, len(log.energies), (log.truncated_weights[-1] if log.truncated_weights else 0.0)
+    return E, sweeps + len(log.energies), (log.truncated_weights[-1] if log.truncated_weights else 0.0)
 
 
 class ServingEngine:
