@@ -170,15 +170,16 @@ struct JacobiParams {
 };
 
 // Pairs the decoupling FP64 sweep of a truncating mixed-precision SVD leaves alone
-// (skip = the squared discard level of the sector, 0: none): both columns below it, or
-// the smaller one below it and under 2^-14 of the larger in norm.  After the FP32 sweeps
-// a pair's coupling is at most a few 1e-6 of the product of its norms, so rotating the
-// second kind would move the larger (kept) column by under 1e-14 of its norm; the
-// smaller column is discarded by the truncation anyway.
+// (skip = the squared discard level of the sector, 0: none): both columns below it.
+// A pair of one kept and one discarded column is always rotated: the columns the FP32
+// sweeps deflated (norm below FP32 resolution) were never decoupled from the kept ones,
+// their couplings can be of the order of the product of the norms, and left in place
+// they would shift the kept values by ~1e-12 of the largest.  Rotations among the
+// discarded columns are the ones skipped: they would shuffle those couplings around
+// within the discarded set instead of removing them.
 template <class T>
 __device__ __forceinline__ bool pair_skipped(T al, T be, T skip) {
-    const T lo = al < be ? al : be, hi = al < be ? be : al;
-    return lo < skip && (hi < skip || lo < T(3.7252902984619140625e-09) * hi);  // 2^-28 in squared norms
+    return al < skip && be < skip;
 }
 
 // Rotation of one column pair by one warp.  With R > 0 (p <= 32 R) every lane

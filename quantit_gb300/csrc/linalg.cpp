@@ -443,9 +443,8 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             if (discard.empty()) {
                 fp64_sweeps(max_sweeps, thr64 ? thr64->p : nullptr, nullptr);
             } else {
-                // one sweep decouples the columns (pairs of two discarded columns, and pairs of
-                // a discarded column with one over 2^14 times larger, stay as they are), then
-                // the columns below tau leave the sweeps with the null ones
+                // one sweep decouples the columns (pairs of two discarded columns stay as they
+                // are), then the columns below tau leave the sweeps with the null ones
                 std::vector<double> skip2(nsec), thr2(nsec);
                 for (int i = 0; i < nsec; ++i) {
                     skip2[i] = discard[i] * discard[i];

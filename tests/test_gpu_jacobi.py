@@ -200,8 +200,10 @@ def test_truncation_aware_fp64_stage_keeps_fp64_accuracy(kernel):
     """A truncation to a quarter of the values (max_size), with every sector's spectrum
     spread over 13 decades: the threshold lies far above FP32 resolution, so the mixed
     path's FP64 stage leaves the columns below half its estimate out of the sweeps
-    (pairs of two of them, and pairs of one with a column over 2^14 times larger, in the
-    decoupling sweep; every pair of theirs afterwards).  The kept values match LAPACK to
+    (pairs of two of them in the decoupling sweep, every pair of theirs afterwards).  A
+    variant that also skipped pairs of a kept column with a discarded one 2^14 times
+    smaller shifted the kept values by up to 7e-12 of the largest: the columns the FP32
+    sweeps deflated are not decoupled from the kept ones.  The kept values match LAPACK to
     1e-12 of the largest, the kept singular vectors match LAPACK's to 1e-10, the kept
     factors are isometries to FP64 precision, and the plain FP64 path keeps the same."""
     rng = np.random.default_rng(97)
