@@ -127,7 +127,16 @@ def test_mixed_dmrg_from_noncanonical_state():
         mps = q.networks.random_bmps(L, D, seed=5)
         opts = q.algorithms.dmrg_options(cutoff=1e-10, convergence_criterion=1e-9, max_bond=D, min_bond=1,
                                          maximum_iterations=20, gemm=gemm, final_energy_fp64=True)
-        out[gemm] = q.algorithms.dmrg(mpo, mps, opts)
+        log = q.algorithms.dmrg_log_sweeptime()
+        out[gemm] = q.algorithms.dmrg(mpo, mps, opts, log)
+        if gemm != "f64":
+            # converged on two consecutive FP64 energies (evaluated once the Ritz value
+            # settled), before the sweep limit; the returned energy is the state's FP64 energy
+            assert len(log.energies) < 20, log.energies
+            e, n2 = q.algorithms.mps_energy(mpo, mps)
+            assert out[gemm] == pytest.approx(e / n2, rel=1e-12)
+            assert log.energies[-1] == out[gemm]
+            assert abs(log.energies[-1] - log.energies[-2]) <= 1e-9 * abs(log.energies[-1])
     for gemm in TC_MODES:
         assert np.isfinite(out[gemm])
         assert abs(out[gemm] - out["f64"]) / L < 1e-7, (gemm, out)
