@@ -182,6 +182,23 @@ __device__ __forceinline__ bool pair_skipped(T al, T be, T skip) {
     return al < skip && be < skip;
 }
 
+// End of a sweep.  The sweep's largest relative coupling |<w_a, w_b>| / (|w_a| |w_b|)
+// among the pairs it rotated is kept as the bits of a non-negative float (0: nothing
+// rotated; a deflation counts as 1).  The sector is done when nothing rotated, or when
+// every rotation was so small that the next sweep has nothing left to do: one-sided
+// Jacobi converges quadratically near the end, so couplings of at most delta before a
+// sweep are of order delta^2 after it, and delta^2 <= 1e-3 tol leaves a margin of 1e3
+// for the constant (small relative gaps between the values).  That saves the sweep
+// which would only have confirmed convergence, and the sweeps that chase rounding noise
+// just above the tolerance.
+constexpr double kSettle = 1e-3;
+template <class T>
+__device__ __forceinline__ bool sweep_converged(int bits, int p) {
+    if (bits == 0) return true;
+    const double d = double(__int_as_float(bits));
+    return d * d <= kSettle * double(Eps<T>::tol(p));
+}
+
 // Rotation of one column pair by one warp.  With R > 0 (p <= 32 R) every lane
 // first loads its R elements of both columns into registers -- one round trip to
 // L2 instead of one per element -- then forms the three inner products, the
@@ -192,7 +209,7 @@ __device__ __forceinline__ bool pair_skipped(T al, T be, T skip) {
 template <class T, int R>
 __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ wb, T *__restrict__ va,
                                             T *__restrict__ vb, int p, int q, int lane, T thr, T *da, T *db,
-                                            T skip) {
+                                            T skip, float &rel) {
     T al = 0, be = 0, ga = 0;
     T x[R > 0 ? R : 1], y[R > 0 ? R : 1];
     if (R > 0) {
@@ -229,10 +246,12 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
             if (za) *da = al;
             if (zb) *db = be;
         }
+        rel = 1.0f;  // a deflation always asks for another sweep
         return true;
     }
     if (pair_skipped(al, be, skip)) return false;
     if (ga == T(0) || fabs(ga) <= Eps<T>::tol(p) * sqrt(al) * sqrt(be)) return false;
+    rel = float(fabs(ga) / (sqrt(al) * sqrt(be)));
     T sn, tau;
     rot_params(al, be, ga, sn, tau);
     if (R > 0) {
@@ -341,10 +360,11 @@ __global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
             T *va = P.rot + sd.rot_off + int64_t(a) * sd.q;
             T *vb = P.rot + sd.rot_off + int64_t(b) * sd.q;
             T *dn = P.dnorm ? P.dnorm + sd.s_off : nullptr;
+            float rel = 0.0f;
             if (!rotate_pair<T, R>(wa, wb, va, vb, sd.p, sd.q, lane, P.defl ? P.defl[s] : T(0), dn ? dn + a : nullptr,
-                                   dn ? dn + b : nullptr, P.skip ? P.skip[s] : T(0)))
+                                   dn ? dn + b : nullptr, P.skip ? P.skip[s] : T(0), rel))
                 continue;
-            if (lane == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
+            if (lane == 0) atomicMax(P.rotated + int64_t(s) * P.max_sweeps + sweep[s], __float_as_int(rel));
         }
         grid.sync();
         for (int s = threadIdx.x; s < nsec; s += blockDim.x) {
@@ -353,9 +373,9 @@ __global__ void __launch_bounds__(JJ) k_jacobi(JacobiParams<T> P) {
             const int qp = q + (q & 1);
             if ((step + 1) % (qp - 1) == 0) {
                 const int sw = sweep[s];
-                const bool rot = ((volatile int *)P.rotated)[int64_t(s) * P.max_sweeps + sw] != 0;
+                const int bits = ((volatile int *)P.rotated)[int64_t(s) * P.max_sweeps + sw];
                 sweep[s] = sw + 1;
-                if (!rot || sw + 1 >= P.max_sweeps) {
+                if (sweep_converged<T>(bits, P.secs[s].p) || sw + 1 >= P.max_sweeps) {
                     done[s] = 1;
                     atomicAdd(&ndone, 1);
                 }
@@ -495,17 +515,21 @@ __device__ __forceinline__ void bj_params_fast(float al, float be, float ga, flo
 // (set to zero, norm 0; dx / dy receive its squared norm before, else stay 0).
 template <class T, int R>
 __device__ __forceinline__ bool bj_rotate(T (&x)[R], T (&y)[R], T &al, T &be, T tol, T thr, T &sn, T &tau, T &dx,
-                                          T &dy, T skip) {
+                                          T &dy, T skip, float &rmax) {
     if (al == T(0) || be == T(0)) return false;
     if (pair_skipped(al, be, skip)) return false;
     const T ga = bj_dot(x, y);
     if (ga == T(0)) return false;
     T t;
     if constexpr (sizeof(T) == 4) {
-        if (fabsf(ga) * rsqrtf(al) * rsqrtf(be) <= tol) return false;
+        const float rel = fabsf(ga) * rsqrtf(al) * rsqrtf(be);
+        if (rel <= tol) return false;
+        rmax = fmaxf(rmax, rel);
         bj_params_fast(al, be, ga, sn, tau, t);
     } else {
-        if (fabs(ga) <= tol * sqrt(al * be)) return false;
+        const double rel = fabs(ga) / sqrt(al * be);
+        if (rel <= tol) return false;
+        rmax = fmaxf(rmax, float(rel));
         rot_params(al, be, ga, sn, tau, t);
     }
 #pragma unroll
@@ -615,7 +639,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
     int *done = reinterpret_cast<int *>(nrm + NP);
     int *sweep = done + nsec;
     int *istart = sweep + nsec;  // nsec + 1 prefix sums of block pairs per step
-    __shared__ int ndone, any_rot, s_unit;
+    __shared__ int ndone, any_rot, s_unit, s_rmax;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool defer_v = P.qbuf != nullptr;
     const int64_t gt = int64_t(blockIdx.x) * NT + tid;
@@ -723,9 +747,13 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                 if (lane == 0) nrm[j] = acc;
             }
             for (int e = tid; e < NP * NP; e += NT) Qs[e] = (e % (NP + 1) == 0) ? T(1) : T(0);
-            if (tid == 0) any_rot = 0;
+            if (tid == 0) {
+                any_rot = 0;
+                s_rmax = 0;
+            }
             __syncthreads();
             bool rotated_any = zeroed;
+            float rmax = zeroed ? 1.0f : 0.0f;  // a deflation always asks for another sweep
             T x[R], y[R], sn, tau;
             if (k == 0) {
                 // intra-block pairs: round-robin over the B columns of each block
@@ -739,7 +767,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                         bj_load(x, cols + u * PP, lane);
                         bj_load(y, cols + v * PP, lane);
                         T al = nrm[u], be = nrm[v], dx = T(0), dy = T(0);
-                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy, skp)) {
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy, skp, rmax)) {
                             if (lane == 0 && dx > T(0)) P.dnorm[sd.s_off + column(u)] = dx;
                             if (lane == 0 && dy > T(0)) P.dnorm[sd.s_off + column(v)] = dy;
                             bj_store(x, cols + u * PP, lane);
@@ -775,7 +803,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     if (mine && valid(j)) {
                         bj_load(y, cols + j * PP, lane);
                         T be = nrm[j], dx = T(0), dy = T(0);
-                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy, skp)) {
+                        if (bj_rotate(x, y, al, be, tol, thr, sn, tau, dx, dy, skp, rmax)) {
                             if (lane == 0 && dx > T(0)) P.dnorm[sd.s_off + column(warp)] = dx;
                             if (lane == 0 && dy > T(0)) P.dnorm[sd.s_off + column(j)] = dy;
                             bj_store(y, cols + j * PP, lane);
@@ -796,7 +824,10 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                     rotated_any = true;
                 }
             }
-            if (rotated_any && lane == 0) any_rot = 1;
+            if (rotated_any && lane == 0) {
+                any_rot = 1;
+                atomicMax(&s_rmax, __float_as_int(rmax > 0.0f ? rmax : 1.0f));
+            }
             __syncthreads();
             if (any_rot) {
                 for (int j = warp; j < NP; j += B) {
@@ -826,7 +857,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
                 } else {
                     bj_apply_v<T, B>(V, q, a, b, na, nbc, Qs, 0, q, tid);
                 }
-                if (tid == 0) P.rotated[int64_t(s) * P.max_sweeps + sweep[s]] = 1;
+                if (tid == 0) atomicMax(P.rotated + int64_t(s) * P.max_sweeps + sweep[s], s_rmax);
             }
             __syncthreads();
         }
@@ -840,9 +871,9 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             const int nbp = nb + (nb & 1);
             if ((step + 1) % (nbp - 1) == 0) {
                 const int sw = sweep[s];
-                const bool rot = ((volatile int *)P.rotated)[int64_t(s) * P.max_sweeps + sw] != 0;
+                const int bits = ((volatile int *)P.rotated)[int64_t(s) * P.max_sweeps + sw];
                 sweep[s] = sw + 1;
-                if (!rot || sw + 1 >= P.max_sweeps) {
+                if (sweep_converged<T>(bits, P.secs[s].p) || sw + 1 >= P.max_sweeps) {
                     done[s] = 1;
                     atomicAdd(&ndone, 1);
                 }
