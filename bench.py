@@ -413,14 +413,20 @@ def serving_section(q, args, n_requests):
     if rate <= 0:
         burst = serving.poisson_requests(args.serving_calibrate, rate=0.0, seed=1, **dist)
         eng = engine()
-        res = eng.run(burst, realtime=False)
+        res = eng.run(burst, realtime=False,
+                      on_done=lambda r: print(f"calibration {r.rid} L={r.L} D={r.D} service={r.service:.1f} s",
+                                              file=sys.stderr, flush=True))
         cap = len(res) / max(r.done for r in res)
         rate = args.serving_load * cap
         out["capacity"] = {"requests": len(res), "solves_per_s": cap,
                            "how": "burst released at once (seed 1); solves / time to the last completion"}
     reqs = serving.poisson_requests(n_requests, rate=rate, seed=0, **dist)
     eng = engine()
-    res = eng.run(reqs, realtime=True)
+
+    def progress(r):
+        print(f"served {r.rid} L={r.L} D={r.D} sweeps={r.sweeps} latency={r.latency:.1f} s "
+              f"service={r.service:.1f} s", file=sys.stderr, flush=True)
+    res = eng.run(reqs, realtime=True, on_done=progress)
     mk = max(r.done for r in res) - min(r.arrival for r in res)
     out.update(serving.summarize([r.latency for r in res], mk, len(res)))
     lat = np.array([r.latency for r in res])

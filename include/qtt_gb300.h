@@ -195,11 +195,9 @@ typedef struct {
     int64_t maximum_iterations;    /* sweeps (default 1000) */
     int32_t gemm_mode;             /* QTT_GEMM_* for the matvecs and environment updates */
     int32_t final_energy_fp64;     /* mixed gemm_mode: use the FP64 <psi|H|psi>/<psi|psi> of the state
-                                      instead of the last Ritz value -- for the returned energy, and
-                                      when convergence_criterion > 0 for the convergence test and the
-                                      log of every sweep whose Ritz value moved by at most 1e-5
-                                      relative (two such FP64 energies in a row decide convergence;
-                                      other sweeps log their Ritz value) (default 1) */
+                                      instead of the last Ritz value -- after every sweep for the
+                                      convergence test and the log when convergence_criterion > 0,
+                                      and for the returned energy (default 1) */
     int32_t lanczos_steps;         /* 1: QuantiT's one-step update (two_sites_update, dmrg.cpp:624-638);
                                       k > 1: k-step Lanczos with full reorthogonalisation (no
                                       reference counterpart; default 1) */

@@ -390,8 +390,6 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
     double E0 = 100000.0;
     const bool fp64_energy = opt.gemm_mode != GEMM_F64 && opt.final_energy_fp64;
     bool last_fp64 = false;  // E0 is the FP64 energy of the current state
-    double prev_ritz = 0.0, prev_fp64 = 0.0;  // mixed path with a criterion: the previous sweep's energies
-    bool have_ritz = false, have_fp64 = false;
     int64_t init_pos = oc;
     const int64_t nh = L - 1;
     const int64_t n_step = nh - 1 + (nh == 1);
@@ -461,33 +459,19 @@ double dmrg(const std::vector<BT> &mpo, std::vector<BT> &mps, int64_t &oc_io, co
         }
         // Mixed path with a criterion: its Ritz values carry the error of the FP32
         // tensor-core accumulation (1e-7 .. 1e-4 relative, growing with the bond dimension
-        // and the chain), under which a tight relative criterion never fires.  The
-        // criterion is tested on FP64 energies of the sweep's state (a contraction of the
-        // whole network in FP64, dearer than a mixed sweep at large D), evaluated once the
-        // Ritz value has settled to within kRitzGate of the previous sweep's: two
-        // consecutive FP64 energies decide convergence; a sweep with an unsettled Ritz
-        // value reports it and starts the FP64 history afresh.
-        constexpr double kRitzGate = 1e-5;
-        const double ritz = E;
-        const bool settled = have_ritz && std::fabs(ritz - prev_ritz) <= kRitzGate * std::fabs(ritz);
-        prev_ritz = ritz;
-        have_ritz = true;
-        last_fp64 = settled;
-        if (settled) {
+        // and along the chain of environment updates), under which a tight relative
+        // criterion never fires; the criterion is tested on the FP64 energy of every
+        // sweep's state (a contraction of the whole network in FP64).
+        {
             double n2 = 1.0;
             const double e = mps_energy(mpo, mps, &n2);
             E = e / n2;
         }
+        last_fp64 = true;
         if (hooks.sweep) hooks.sweep(hooks.user, it, E, secs, trunc, mps, oc);
+        const double prev = E0;
         E0 = E;
-        if (!settled) {
-            have_fp64 = false;
-            continue;
-        }
-        const bool converged = have_fp64 && !(std::fabs((E - prev_fp64) / E) > opt.convergence_criterion);
-        prev_fp64 = E;
-        have_fp64 = true;
-        if (converged) break;
+        if (!(std::fabs((E0 - prev) / E0) > opt.convergence_criterion)) break;
     }
     // `it`: the sweep that met the criterion, or maximum_iterations (dmrg.cpp:238-270)
     if (oc != init_pos) {

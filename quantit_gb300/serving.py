@@ -188,9 +188,10 @@ class ServingEngine:
         self.peak_concurrency = 0
         self.peak_memory = 0
 
-    def run(self, requests, realtime=True):
+    def run(self, requests, realtime=True, on_done=None):
         """Serve ``requests`` (released at their arrival times when ``realtime``,
-        all at once otherwise); returns the results in request order."""
+        all at once otherwise); returns the results in request order.  ``on_done(result)``
+        is called on the worker thread as each request finishes."""
         reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
         n = len(reqs)
         results = {}
@@ -217,6 +218,11 @@ class ServingEngine:
                 except Exception as e:  # reported per request, the server keeps going
                     res.error = f"{type(e).__name__}: {e}"
                 res.done = time.perf_counter() - t0
+                if on_done is not None:
+                    try:
+                        on_done(res)
+                    except Exception:  # a progress callback never stops the server
+                        pass
                 with cond:
                     state["in_flight"] -= 1
                     state["mem"] -= res.footprint

@@ -64,13 +64,22 @@ def test_device_planner_matches_oracle_and_host(mods):
 
 @pytest.mark.parametrize("D", [512, 2048])
 def test_device_planner_on_the_theta_pair(D):
-    """Config-2 operands (17 charge sectors per bond leg, ~10^3 blocks each) contracted
-    over one and two legs, and A against its conjugate over two and three legs."""
+    """Config-2 operands (17 charge sectors per bond leg, ~10^3 blocks each): planned
+    over one and two legs of A against B and over two and three legs of A against its
+    conjugate (structure only: the two-leg product has D^4 elements), and computed with
+    data where the product is small enough."""
     A, B = NET.theta_pair(D, seed=3)
+    sa = A.copy_structure().set_block_structure(A.block_indices())
+    sb = B.copy_structure().set_block_structure(B.block_indices())
+    sc = sa.conj()
+    plans = [lambda: sa.tensordot(sb, ([3], [0])), lambda: sa.tensordot(sb, ([2, 3], [1, 0])),
+             lambda: sa.tensordot(sc, ([1, 2], [1, 2])), lambda: sa.tensordot(sc, ([0, 1, 2], [0, 1, 2]))]
+    for fn in plans:
+        h, d, st = _host_and_device(fn)
+        assert h.block_indices() == d.block_indices()
+        assert st["device_calls"] == 1 and st["device_fallbacks"] == 0
     Ac = A.conj()
-    cases = [lambda: A.tensordot(B, ([3], [0])), lambda: A.tensordot(B, ([2, 3], [1, 0])),
-             lambda: A.tensordot(Ac, ([1, 2], [1, 2])), lambda: A.tensordot(Ac, ([0, 1, 2], [0, 1, 2]))]
-    for fn in cases:
+    for fn in (lambda: A.tensordot(B, ([2, 3], [1, 0])), lambda: A.tensordot(Ac, ([0, 1, 2], [0, 1, 2]))):
         h, d, st = _host_and_device(fn)
         _bit_identical(h, d)
         assert st["device_calls"] == 1 and st["device_fallbacks"] == 0

@@ -130,8 +130,8 @@ def test_mixed_dmrg_from_noncanonical_state():
         log = q.algorithms.dmrg_log_sweeptime()
         out[gemm] = q.algorithms.dmrg(mpo, mps, opts, log)
         if gemm != "f64":
-            # converged on two consecutive FP64 energies (evaluated once the Ritz value
-            # settled), before the sweep limit; the returned energy is the state's FP64 energy
+            # converged on consecutive FP64 energies before the sweep limit; the returned
+            # energy is the state's FP64 energy
             assert len(log.energies) < 20, log.energies
             e, n2 = q.algorithms.mps_energy(mpo, mps)
             assert out[gemm] == pytest.approx(e / n2, rel=1e-12)
