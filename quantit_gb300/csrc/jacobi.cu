@@ -184,7 +184,8 @@ __device__ __forceinline__ bool pair_skipped(T al, T be, T skip) {
 
 // End of a sweep.  The sweep's largest relative coupling |<w_a, w_b>| / (|w_a| |w_b|)
 // among the pairs it rotated is kept as the bits of a non-negative float (0: nothing
-// rotated; a deflation counts as 1).  The sector is done when nothing rotated, or when
+// rotated; a deflation alone counts as the smallest normal float: zeroing a null
+// column removes its couplings and changes no other column).  The sector is done when nothing rotated, or when
 // every rotation was so small that the next sweep has nothing left to do: one-sided
 // Jacobi converges quadratically near the end, so couplings of at most delta before a
 // sweep are of order delta^2 after it, and delta^2 <= 1e-3 tol leaves a margin of 1e3
@@ -246,7 +247,7 @@ __device__ __forceinline__ bool rotate_pair(T *__restrict__ wa, T *__restrict__ 
             if (za) *da = al;
             if (zb) *db = be;
         }
-        rel = 1.0f;  // a deflation always asks for another sweep
+        rel = 1.17549435e-38f;  // a deflation removes couplings and adds none: it alone settles
         return true;
     }
     if (pair_skipped(al, be, skip)) return false;
@@ -753,7 +754,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             }
             __syncthreads();
             bool rotated_any = zeroed;
-            float rmax = zeroed ? 1.0f : 0.0f;  // a deflation always asks for another sweep
+            float rmax = zeroed ? 1.17549435e-38f : 0.0f;  // a deflation removes couplings and adds none
             T x[R], y[R], sn, tau;
             if (k == 0) {
                 // intra-block pairs: round-robin over the B columns of each block
@@ -826,7 +827,7 @@ __global__ void __launch_bounds__(B * 32) k_bjacobi(BJacobiParams<T> P) {
             }
             if (rotated_any && lane == 0) {
                 any_rot = 1;
-                atomicMax(&s_rmax, __float_as_int(rmax > 0.0f ? rmax : 1.0f));
+                atomicMax(&s_rmax, __float_as_int(rmax > 0.0f ? rmax : 1.17549435e-38f));
             }
             __syncthreads();
             if (any_rot) {

@@ -214,7 +214,7 @@ int svd_deflation() { return g_svd_deflation; }
 
 namespace {
 std::atomic<int> g_planner{2};
-std::atomic<int64_t> g_planner_auto{512};
+std::atomic<int64_t> g_planner_auto{3000};
 std::mutex g_plan_mu;
 int64_t g_plan_calls[3] = {0, 0, 0};
 double g_plan_secs[2] = {0.0, 0.0};
