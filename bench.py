@@ -82,7 +82,7 @@ def parse():
     p.add_argument("--svd-deflation", type=int, default=None,
                    help="1/0: numerically null columns leave the sector-SVD sweeps of a truncating svd")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving", "contraction", "svd"],
+    p.add_argument("--workload", default="dmrg", choices=["dmrg", "serving", "contraction", "svd", "planner"],
                    help="dmrg: the D=2048 sweep line (with a short serving section); serving: the full "
                         "Poisson request stream of XXZ solves (L in 16..128, D in 32..512); contraction: the "
                         "synthetic theta-pair contraction + sector-SVD truncation microbench at D; svd: the "
@@ -536,6 +536,44 @@ def svd_workload(q, args):
             "roofline": dict(roofline("svd", kinds["svd"], peaks(), args.mode, {}),
                              stages=svd_stages(kinds, args.mode, {})),
             "kernel_time_ms": {k: v["ms"] for k, v in timed_kinds(kinds).items()}}
+
+
+def planner_workload(q, args):
+    """Planner time per contraction, host merge-join against the device planner, on
+    structure-only U(1)xU(1) rank-3 tensors A[a, s, b] with (2k+1)^2 charge sectors per
+    bond leg (2 states each) and 4 physical sectors: A.B over one leg and A.A* over two,
+    each planned 10 times after one untimed call (host wall time, planner_stats)."""
+    from quantit_gb300.conserved import ZZ
+    shifts = [(0, 0), (-1, -1), (-1, 1), (-2, 0)]
+    physi = [(1, ZZ(-a, -b)) for a, b in [(0, 0), (1, 1), (1, -1), (2, 0)]]
+    rows = []
+    for k in (4, 8, 12, 16, 24, 31):
+        grid = [(i, j) for i in range(-k, k + 1) for j in range(-k, k + 1)]
+        pos = {g: n for n, g in enumerate(grid)}
+        legs = [[(2, ZZ(i, j)) for i, j in grid], physi, [(2, ZZ(-i, -j)) for i, j in grid]]
+        blocks = [(a, si, pos[(g[0] + d[0], g[1] + d[1])]) for a, g in enumerate(grid)
+                  for si, d in enumerate(shifts) if (g[0] + d[0], g[1] + d[1]) in pos]
+        A = q.btensor(legs, ZZ(0, 0)).set_block_structure(blocks)
+        B = q.btensor(legs, ZZ(0, 0)).set_block_structure(blocks)
+        Ac = A.conj()
+        row = {"sectors_per_bond_leg": len(grid), "blocks_per_operand": len(blocks)}
+        for name, fn in (("AB", lambda: A.tensordot(B, ([2], [0]))), ("AAc", lambda: A.tensordot(Ac, ([0, 1], [0, 1])))):
+            for mode in ("host", "device"):
+                q.set_planner(mode)
+                fn()
+                q.planner_stats(reset=True)
+                for _ in range(10):
+                    fn()
+                st = q.planner_stats(reset=True)
+                row[f"{name}_{mode}_ms"] = 1e3 * (st["host_s"] + st["device_s"]) / 10
+                row[f"{name}_{mode}_fallbacks"] = st["device_fallbacks"]
+        rows.append(row)
+    q.set_planner(args.planner)
+    last = rows[-1]
+    return {"metric": "ms per contraction plan (device planner, largest case)", "value": last["AB_device_ms"],
+            "unit": "ms", "n_gpus": 1, "steps": 10, "warmup": 1, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+            "config": {"workload": "tensordot planning of structure-only U(1)xU(1) rank-3 tensors"}, "rows": rows}
 
 
 def contraction_workload(q, args):
@@ -1099,8 +1137,9 @@ def main():
     q.set_planner(args.planner)
     if args.svd_deflation is not None:
         q.set_svd_deflation(bool(args.svd_deflation))
-    if args.workload in ("contraction", "svd"):
-        line = (contraction_workload if args.workload == "contraction" else svd_workload)(q, args)
+    if args.workload in ("contraction", "svd", "planner"):
+        line = {"contraction": contraction_workload, "svd": svd_workload,
+                "planner": planner_workload}[args.workload](q, args)
         if rank == 0:
             print(json.dumps(line))
         if world > 1:
