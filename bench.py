@@ -335,6 +335,11 @@ def roofline(kind, st, P, mode, peaks_cache):
 
 
 WORK_ONLY = ("jacobi_fp32", "jacobi_fp64")   # statistics kinds that carry FLOPs but no time
+# DRAM bytes (read + write) of one mixed-path decomposition of the mid-cylinder theta at
+# D = 2048, summed over its kernels from one ncu capture (cold cache, serialised launches;
+# profiles/svd_mixed_cylinder_theta_D2048.md).  The decomposition is the svd class's
+# largest launch in the cylinder sweep.
+SVD_TRAFFIC_MID_THETA = 5.34e8
 
 
 def timed_kinds(kinds):
@@ -918,6 +923,9 @@ def cylinder_main(args, rank, world, local):
     line["roofline"] = roofline(dom, kinds[dom], P, args.mode, pc)
     if dom == "svd":
         line["roofline"]["stages"] = svd_stages(kinds, args.mode, pc)
+        if args.mode == "tf32x3" and args.D == 2048:
+            line["roofline"]["traffic"] = SVD_TRAFFIC_MID_THETA
+            line["roofline"]["traffic_of"] = "the mid-bond decomposition (ncu, profiles/)"
     line["roofline_gemm"] = roofline("gemm", kinds["gemm"], P, args.mode, pc)
     line["kernel_time_ms"] = {k: round(v["ms"], 1) for k, v in timed_kinds(kinds).items()}
     line["sweeps"] = {"times_s": [round(x, 3) for x in log.time_list], "middle_bond": log.bond_list,
@@ -997,7 +1005,7 @@ def slim_cylinder_line(line):
     roofline objects and the serving summary, with floats at 4 significant digits
     (energies at 12) and without the per-sweep lists and notes, so the line stays
     under 3 KB; the full line goes to stderr."""
-    keep = ("kernel", "bound", "achieved", "peak", "unit", "frac", "traffic", "per_launch_ms")
+    keep = ("kernel", "bound", "achieved", "peak", "unit", "frac", "traffic", "traffic_of", "per_launch_ms")
     out = {k: line[k] for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data")}
     cfg = line["config"]
