@@ -208,6 +208,20 @@ void launch_svd_refine(const float *rot32, const double *w64, double *w1, double
 // out[s_off + j] = squared norm (FP64) of column j of every sector's work matrix (f32:
 // FP32 work matrices)
 void launch_col_norms(const void *W, const SectorDesc *secs, int nsec, int max_q, double *out, int f32);
+// Column copies dst[dst_off + r] = src[src_off + r], r < len (FP64), one task per column:
+// the gather and scatter of the kept columns around the restricted FP64 sweeps.
+struct ColCopy {
+    int64_t src_off, dst_off;
+    int32_t len, pad;
+};
+void launch_col_copy(const double *src, double *dst, const std::vector<ColCopy> &cols);
+// Vn = Vg R per sector (FP64): Vg (vrows x k at vg_off, column-major), R (k x k at r_off),
+// Vn (vrows x k at vn_off).
+struct RotProduct {
+    int64_t vg_off, r_off, vn_off;
+    int32_t vrows, k;
+};
+void launch_rot_product(const double *vg, const double *r, double *vn, const std::vector<RotProduct> &t);
 // Segment = one input block (rows x cols at src_off) placed at rows [r0, r0+rows),
 // cols [c0, c0+cols) of sector `sector`.
 struct PackEntry {

@@ -452,8 +452,79 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
                 }
                 const double *dskip = static_cast<const double *>(upload(skip2.data(), skip2.size() * 8));
                 fp64_sweeps(1, thr64->p, dskip);
-                const double *dthr = static_cast<const double *>(upload(thr2.data(), thr2.size() * 8));
-                fp64_sweeps(max_sweeps, dthr, nullptr);
+                // The remaining sweeps run on the kept columns only (norm above the discard
+                // level after the decoupling sweep), gathered into compact sector matrices
+                // W_k (p x K) with a fresh rotation R (K x K): V's kept columns become V_k R
+                // afterwards.  The discarded columns keep their decoupled state; they lie
+                // below the truncation's threshold, which the caller checks.
+                BufPtr cn = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * 8);
+                launch_col_norms(w1->p, dsec64, nsec, max_q, static_cast<double *>(cn->p), 0);
+                std::vector<double> n2c(size_t(std::max<int64_t>(stot, 1)));
+                cuda_check(cudaMemcpyAsync(n2c.data(), cn->p, size_t(stot) * 8, cudaMemcpyDeviceToHost, ctx().stream),
+                           "cudaMemcpyAsync(column norms)");
+                cuda_check(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+                std::vector<SectorDesc> dk(nsec);
+                std::vector<int> kslots(1, 0);
+                std::vector<ColCopy> wgather, vgather, wscatter, vscatter, dscatter;
+                std::vector<RotProduct> rp;
+                int64_t kw = 0, kr = 0, kv = 0, ks = 0;
+                int kmax_steps = 1;
+                for (int i = 0; i < nsec; ++i) {
+                    const SectorDesc &d = D.desc[i];
+                    SectorDesc c{};
+                    c.m = d.m;
+                    c.n = d.n;
+                    c.p = d.p;
+                    c.w_off = kw;
+                    c.rot_off = kr;
+                    c.s_off = ks;
+                    int k = 0;
+                    for (int j = 0; j < d.q; ++j) {
+                        if (!(n2c[size_t(d.s_off + j)] > thr2[i])) continue;
+                        wgather.push_back({d.w_off + int64_t(j) * d.p, kw + int64_t(k) * d.p, d.p, 0});
+                        vgather.push_back({d.rot_off + int64_t(j) * d.q, kv + int64_t(k) * d.q, d.q, 0});
+                        wscatter.push_back({kw + int64_t(k) * d.p, d.w_off + int64_t(j) * d.p, d.p, 0});
+                        vscatter.push_back({kv + int64_t(k) * d.q, d.rot_off + int64_t(j) * d.q, d.q, 0});
+                        dscatter.push_back({ks + k, d.s_off + j, 1, 0});
+                        ++k;
+                    }
+                    c.q = k;
+                    if (k > 0) rp.push_back({kv, kr, kv, d.q, k});
+                    kw += int64_t(d.p) * k;
+                    kr += int64_t(k) * k;
+                    kv += int64_t(d.q) * k;
+                    ks += k;
+                    const int kp = k + (k & 1);
+                    if (kp >= 2) kmax_steps = std::max(kmax_steps, kp - 1);
+                    kslots.push_back(kslots.back() + kp / 2);
+                    dk[i] = c;
+                }
+                BufPtr wk = dev_alloc(size_t(std::max<int64_t>(kw, 1)) * 8);
+                BufPtr rk = dev_alloc(size_t(std::max<int64_t>(kr, 1)) * 8);
+                BufPtr vg = dev_alloc(size_t(std::max<int64_t>(kv, 1)) * 8);
+                BufPtr vn = dev_alloc(size_t(std::max<int64_t>(kv, 1)) * 8);
+                launch_col_copy(static_cast<const double *>(w1->p), static_cast<double *>(wk->p), wgather);
+                launch_col_copy(static_cast<const double *>(vbuf->p), static_cast<double *>(vg->p), vgather);
+                const SectorDesc *ddk = upload_vec(dk);
+                const int *dkslots = upload_vec(kslots);
+                const size_t vbk = jacobi_vwork_bytes(nsec, ks, kmax_steps, max_sweeps, 0);
+                BufPtr vworkk = dev_alloc(vbk);
+                // numerically null columns (the FP64 null level of each sector) still leave the
+                // sweeps; their squared norms land in a compact dnorm and go back to theirs
+                BufPtr dnk;
+                if (deflate) {
+                    dnk = dev_alloc(size_t(std::max<int64_t>(ks, 1)) * 8);
+                    cuda_check(cudaMemsetAsync(dnk->p, 0, size_t(std::max<int64_t>(ks, 1)) * 8, ctx().stream),
+                               "cudaMemsetAsync(compact dnorm)");
+                }
+                launch_jacobi(wk->p, rk->p, ddk, dkslots, nsec, kmax_steps, max_sweeps, sw64, sw64 + nsec, 0, max_p, ks,
+                              vworkk->p, vbk, deflate ? thr64->p : nullptr, deflate ? dnk->p : nullptr, nullptr);
+                launch_rot_product(static_cast<const double *>(vg->p), static_cast<const double *>(rk->p),
+                                   static_cast<double *>(vn->p), rp);
+                launch_col_copy(static_cast<const double *>(wk->p), static_cast<double *>(w1->p), wscatter);
+                launch_col_copy(static_cast<const double *>(vn->p), static_cast<double *>(vbuf->p), vscatter);
+                if (deflate) launch_col_copy(static_cast<const double *>(dnk->p), static_cast<double *>(dnorm->p), dscatter);
+                // the compact buffers are released in stream order after the copies above
             }
             fw = w1->p;
             fr = vbuf->p;

@@ -147,7 +147,31 @@ __global__ void k_col_norms(const T *__restrict__ W, const SectorDesc *__restric
     if (lane == 0) out[sd.s_off + col] = acc;
 }
 
+__global__ void __launch_bounds__(256) k_col_copy(const double *__restrict__ src, double *__restrict__ dst,
+                                                  const ColCopy *__restrict__ cc, int n) {
+    for (int c = blockIdx.x; c < n; c += gridDim.x) {
+        const ColCopy e = cc[c];
+        for (int r = threadIdx.x; r < e.len; r += blockDim.x) dst[e.dst_off + r] = src[e.src_off + r];
+    }
+}
+
 }  // namespace
+
+void launch_col_copy(const double *src, double *dst, const std::vector<ColCopy> &cols) {
+    if (cols.empty()) return;
+    const ColCopy *d = upload_vec(cols);
+    const int grid = int(std::min<size_t>(cols.size(), 8192));
+    k_col_copy<<<grid, 256, 0, ctx().stream>>>(src, dst, d, int(cols.size()));
+    count_launch();
+    cuda_check(cudaGetLastError(), "column copy launch");
+}
+
+void launch_rot_product(const double *vg, const double *r, double *vn, const std::vector<RotProduct> &t) {
+    std::vector<SecGemm> g;
+    for (const RotProduct &e : t)
+        g.push_back({e.vg_off, e.r_off, e.vn_off, e.vrows, e.k, e.k, e.vrows, e.k, e.vrows, 0, 0, 0, 0});
+    secgemm(vg, r, vn, g, ctx().stream);
+}
 
 void launch_col_norms(const void *W, const SectorDesc *secs, int nsec, int max_q, double *out, int f32) {
     if (nsec <= 0 || max_q <= 0) return;
