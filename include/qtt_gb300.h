@@ -299,7 +299,8 @@ int qtt_svd_dense_noalloc(const double *a, int64_t m, int64_t n, double *u, doub
  * 4 sector pack (bytes), 5 the FP64 stage of the mixed path's sector SVDs (time only; part
  * of kind 2), 6 / 7 the FLOPs the sector SVDs' Jacobi sweeps performed in FP32 / FP64
  * (work only: sweeps x (6 p q^2 + 3 q^3) per p x q sector, plus 8 q^3 + 2 p q^2 for the
- * mixed path's FP64 refinement products). */
+ * mixed path's FP64 refinement products; under a truncation the mixed path's FP64 sweeps
+ * after the first run on the K kept columns: 6 p K^2 + 3 K^3 each, plus 2 q K^2). */
 int qtt_stats_enable(int on);
 int qtt_stats_reset(void);
 int qtt_stats_get(int kind, double *ms, double *work, int64_t *launches);

@@ -379,6 +379,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
         // >= 4 eps32 ||W_s|| carries FP32 rounding noise of at most a quarter of itself.  The
         // truncation is checked against tau all the same (svd_truncated).
         std::vector<double> discard, null2;
+        std::vector<int> kept_cols;  // discard path: columns of each sector's compact restricted sweeps
         TruncHint &th = trunc_hint();
         if (f32 && deflate && th.allow_discard && th.max_size > 0) {
             BufPtr cn = dev_alloc(size_t(std::max<int64_t>(stot, 1)) * 8);
@@ -489,6 +490,7 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
                         ++k;
                     }
                     c.q = k;
+                    kept_cols.push_back(k);
                     if (k > 0) rp.push_back({kv, kr, kv, d.q, k});
                     kw += int64_t(d.p) * k;
                     kr += int64_t(k) * k;
@@ -538,26 +540,35 @@ void run_decomp(const BT &t, Decomp &D, int mode, int upper) {
             auto ev = std::shared_ptr<CUevent_st>(raw, [](cudaEvent_t e) { cudaEventDestroy(e); });
             std::vector<std::pair<double, double>> pq;
             for (const SectorDesc &d : D.desc) pq.push_back({double(d.p), double(d.q)});
-            auto flops = [ev, pq, nsec](const BufPtr &b, int extra, bool refine) {
+            // kc (discard path): the recorded sweeps ran on kc[i] kept columns after one
+            // decoupling sweep over the whole sector, and V's kept columns took one product
+            auto flops = [ev, pq, nsec](const BufPtr &b, bool refine, const std::vector<int> &kc) {
                 cudaEventSynchronize(ev.get());
                 std::vector<int> sw(size_t(std::max(nsec, 1)), 0);
                 cudaMemcpy(sw.data(), b->p, size_t(nsec) * sizeof(int), cudaMemcpyDeviceToHost);
                 double f = 0.0;
                 for (int i = 0; i < nsec; ++i) {
                     const double P = pq[i].first, Q = pq[i].second;
-                    f += double(sw[i] + extra) * (6.0 * P * Q * Q + 3.0 * Q * Q * Q);
+                    if (kc.empty()) {
+                        f += double(sw[i]) * (6.0 * P * Q * Q + 3.0 * Q * Q * Q);
+                    } else {
+                        const double K = kc[size_t(i)];
+                        f += 6.0 * P * Q * Q + 3.0 * Q * Q * Q;
+                        f += double(sw[i]) * (6.0 * P * K * K + 3.0 * K * K * K) + 2.0 * Q * K * K;
+                    }
                     if (refine) f += 8.0 * Q * Q * Q + 2.0 * P * Q * Q;
                 }
                 return f;
             };
             if (f32) {
                 BufPtr b32 = ibuf, b64 = ibuf64;
-                const int extra = discard.empty() ? 0 : 1;
-                stats_defer_work(ST_JAC32, [flops, b32] { return flops(b32, 0, false); });
-                stats_defer_work(ST_JAC64, [flops, b64, extra] { return flops(b64, extra, true); });
+                const std::vector<int> none, kc = kept_cols;
+                stats_defer_work(ST_JAC32, [flops, b32, none] { return flops(b32, false, none); });
+                stats_defer_work(ST_JAC64, [flops, b64, kc] { return flops(b64, true, kc); });
             } else {
                 BufPtr b = ibuf;
-                stats_defer_work(ST_JAC64, [flops, b] { return flops(b, 0, false); });
+                const std::vector<int> none;
+                stats_defer_work(ST_JAC64, [flops, b, none] { return flops(b, false, none); });
             }
         }
         BufPtr permbuf;

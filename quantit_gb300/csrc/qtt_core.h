@@ -408,7 +408,8 @@ inline void tc_error_raise() {
 // ST_JAC32 / ST_JAC64: work only (no time): the FLOPs the sector SVDs' Jacobi sweeps
 // performed in FP32 and in FP64 (sweeps x (6 p q^2 + 3 q^3) per p x q sector, the
 // one-sided Jacobi count; the FP64 count adds the mixed path's Newton-Schulz and W V
-// products, 8 q^3 + 2 p q^2).
+// products, 8 q^3 + 2 p q^2, and counts its sweeps after the decoupling one on the K kept
+// columns, plus their V product 2 q K^2).
 enum StatKind : int {
     ST_GEMM = 0,
     ST_PERMUTE = 1,
