@@ -104,7 +104,7 @@ def parse():
                    help="serial FP64 baseline on every k-th request of the stream")
     p.add_argument("--serving-fp64-budget", type=float, default=300.0,
                    help="stop the serial FP64 sample once this many seconds are spent")
-    p.add_argument("--planner", default="auto", choices=["host", "device", "auto"],
+    p.add_argument("--planner", default="host", choices=["host", "device", "auto"],
                    help="block-sparsity planner of the contractions (auto: device for >= 3000 blocks in the two operands)")
     p.add_argument("--jacobi", default="block", choices=["block", "scalar"],
                    help="sector-SVD Jacobi kernel (block-cyclic where it fits, or scalar)")

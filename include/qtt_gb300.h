@@ -85,7 +85,7 @@ int qtt_set_svd_deflation(int on);
  * sources/btensor.cpp:783-883,1998-2110): mode 0 plans on the host, 1 on the device
  * wherever the device planner's limits allow (at most 16384 blocks per operand, keys
  * within 63 bits, at least one contracted leg), 2 on the device for contractions with
- * at least auto_blocks blocks in the two operands together (default: mode 2, 3000).
+ * at least auto_blocks blocks in the two operands together (default: mode 0; auto_blocks 3000).
  * Both emit the same output block list and pair order, bit for bit.  Inside CUDA-graph
  * capture the host plans. */
 int qtt_set_planner(int mode, int64_t auto_blocks);

@@ -32,10 +32,10 @@ def set_svd_deflation(on):
     call("qtt_set_svd_deflation", 1 if on else 0)
 
 
-def set_planner(mode="auto", auto_blocks=3000):
-    """Block-sparsity planner of tensordot: "host", "device" (wherever the device
-    planner's limits allow) or "auto" (device for contractions of at least
-    ``auto_blocks`` blocks in both operands together; the default)."""
+def set_planner(mode="host", auto_blocks=3000):
+    """Block-sparsity planner of tensordot: "host" (the default), "device" (wherever the
+    device planner's limits allow) or "auto" (device for contractions of at least
+    ``auto_blocks`` blocks in both operands together)."""
     from ._lib import call
     modes = {"host": 0, "device": 1, "auto": 2}
     if mode not in modes:

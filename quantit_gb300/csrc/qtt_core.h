@@ -381,9 +381,9 @@ std::string autotune_report();
 // Persistent tensor-core GEMM for launches of at least two tiles per SM (on by default).
 void set_persistent_gemm(int on);
 int persistent_gemm();
-// Block-sparsity planner of tensordot: 0 host merge-join, 1 device (planner.cu)
-// wherever its limits allow, 2 device for contractions of at least
-// planner_auto_blocks() blocks in the two operands together (the default).
+// Block-sparsity planner of tensordot: 0 host merge-join (the default), 1 device
+// (planner.cu) wherever its limits allow, 2 device for contractions of at least
+// planner_auto_blocks() blocks in the two operands together.
 void set_planner(int mode, int64_t auto_blocks);
 int planner_mode();
 int64_t planner_auto_blocks();

@@ -213,7 +213,7 @@ void set_svd_deflation(int on) { g_svd_deflation = on ? 1 : 0; }
 int svd_deflation() { return g_svd_deflation; }
 
 namespace {
-std::atomic<int> g_planner{2};
+std::atomic<int> g_planner{0};
 std::atomic<int64_t> g_planner_auto{3000};
 std::mutex g_plan_mu;
 int64_t g_plan_calls[3] = {0, 0, 0};

@@ -27,7 +27,7 @@ def _host_and_device(fn):
         d = fn()
         st = q.planner_stats(reset=True)
     finally:
-        q.set_planner("auto", 3000)
+        q.set_planner("host", 3000)
     return h, d, st
 
 
@@ -103,7 +103,7 @@ def test_device_planner_structure_only_and_errors():
                 sa.tensordot(sb, ([1], [2]))
             msgs.append(str(e.value))
         finally:
-            q.set_planner("auto", 3000)
+            q.set_planner("host", 3000)
     assert msgs[0] == msgs[1]
 
 
@@ -124,7 +124,7 @@ def test_dmrg_energies_identical_with_either_planner():
                               log)
             out[mode] = (list(log.energies), [t.blocks() for t in mps], q.planner_stats(reset=True))
         finally:
-            q.set_planner("auto", 3000)
+            q.set_planner("host", 3000)
     assert out["host"][0] == out["device"][0]
     for th, td in zip(out["host"][1], out["device"][1]):
         assert [k for k, _ in th] == [k for k, _ in td]

@@ -253,7 +253,7 @@ def test_tuning_switches_and_dmrg_options_round_trip():
         q.set_planner("gpu")
     with pytest.raises(ValueError):
         q.set_planner("auto", -1)
-    q.set_planner("auto", 3000)   # the default
+    q.set_planner("host", 3000)   # the default
     st = q.planner_stats(reset=True)
     assert set(st) == {"host_calls", "device_calls", "device_fallbacks", "host_s", "device_s"}
     o = q.algorithms.dmrg_options(gemm="bf16x3", lanczos_steps=4, cuda_graphs=False, svd_warm_start=False,
