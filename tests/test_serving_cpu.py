@@ -89,3 +89,26 @@ def test_footprint_grows_with_size():
     c = serving.footprint_bytes(64, 64)
     assert 0 < a < b < c
     assert serving.footprint_bytes(128, 512) < 40 * 2 ** 30
+
+
+def test_ramp_stages():
+    """A random start is swept at D/4 and D/2 (where at least 32) before D."""
+    assert serving.ramp_stages(512) == [128, 256, 512]
+    assert serving.ramp_stages(128) == [32, 64, 128]
+    assert serving.ramp_stages(64) == [32, 64]
+    assert serving.ramp_stages(32) == [32]
+
+
+def test_results_carry_the_solver_truncated_weight():
+    reqs = [serving.SolveRequest(i, 8, 1.0, 8, i) for i in range(3)]
+    eng = serving.ServingEngine(slots=2, memory_budget=10 ** 9, footprint=lambda r: 1,
+                                solver=lambda r, **k: (-1.0 - r.rid, 2, 1e-9 * (r.rid + 1)))
+    seen = []
+    res = eng.run(reqs, realtime=False, on_done=lambda r: seen.append(r.rid))
+    assert sorted(seen) == [0, 1, 2]
+    assert [r.truncated_weight for r in res] == [1e-9, 2e-9, 3e-9]
+    assert [r.energy for r in res] == [-1.0, -2.0, -3.0]
+    # a two-value solver leaves the truncated weight unknown
+    eng2 = serving.ServingEngine(slots=1, memory_budget=10 ** 9, footprint=lambda r: 1, solver=lambda r, **k: (-1.0, 1))
+    import math
+    assert all(math.isnan(r.truncated_weight) for r in eng2.run(reqs[:1], realtime=False))
