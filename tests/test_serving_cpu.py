@@ -106,7 +106,7 @@ def test_results_carry_the_solver_truncated_weight():
     seen = []
     res = eng.run(reqs, realtime=False, on_done=lambda r: seen.append(r.rid))
     assert sorted(seen) == [0, 1, 2]
-    assert [r.truncated_weight for r in res] == [1e-9, 2e-9, 3e-9]
+    assert [r.truncated_weight for r in res] == [1e-9 * (i + 1) for i in range(3)]
     assert [r.energy for r in res] == [-1.0, -2.0, -3.0]
     # a two-value solver leaves the truncated weight unknown
     eng2 = serving.ServingEngine(slots=1, memory_budget=10 ** 9, footprint=lambda r: 1, solver=lambda r, **k: (-1.0, 1))
