@@ -92,9 +92,9 @@ def parse():
     p.add_argument("--state-file", default=None, help="svd workload: read the theta instead of sweeping")
     p.add_argument("--serving-requests", type=int, default=None,
                    help="requests of the serving stream (default: 200 for --workload serving, 0 otherwise)")
-    p.add_argument("--serving-rate", type=float, default=0.25,
-                   help="Poisson arrival rate (requests/s), below the ~0.38 solves/s the full distribution "
-                        "saturates at; <= 0: --serving-load x the capacity measured on a burst first")
+    p.add_argument("--serving-rate", type=float, default=0.0,
+                   help="Poisson arrival rate (requests/s); <= 0 (the default): --serving-load x the capacity "
+                        "measured on a burst first, so that the stream runs below saturation")
     p.add_argument("--serving-load", type=float, default=0.7, help="offered load of the automatic rate")
     p.add_argument("--serving-calibrate", type=int, default=48, help="requests of the capacity burst")
     p.add_argument("--serving-slots", type=int, default=8)
