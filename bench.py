@@ -850,7 +850,7 @@ def reference_arm_cylinder(args, cfg):
     return {"metric": METRIC, "value": est, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(np.mean([t for _, t in flat[args.warmup:]])) * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": cfg, "impl": "reference",
+            "data": "synthetic", "config": slim_config(cfg), "impl": "reference",
             "cpu_baseline": {"value": est, "unit": UNIT, "cores": host["nproc"], "kind": "port", "sample": sample,
                              "one_thread": {"value": est1, "unit": UNIT, "cores": 1,
                                             "sample": f"bond {bmid}: {t1:.2f} s at 1 BLAS thread against "
@@ -1000,6 +1000,14 @@ def sig(x, n=4):
     return x
 
 
+def slim_config(cfg):
+    """The printed config of the cylinder workload, the same for both arms (the
+    arithmetic is in `dtype`)."""
+    return {"workload": cfg["workload"], "L": cfg["L"], "D": cfg["D"], "cutoff": cfg["cutoff"],
+            "mpo": "compressed to bond dim 20", "update": "one-step Lanczos", "l2": "working set >> L2",
+            "parallelism": cfg["parallelism"]}
+
+
 def slim_cylinder_line(line):
     """The printed line: every key of the contract, the comparison with FP64, the
     roofline objects and the serving summary, with floats at 4 significant digits
@@ -1008,10 +1016,7 @@ def slim_cylinder_line(line):
     keep = ("kernel", "bound", "achieved", "peak", "unit", "frac", "traffic", "traffic_of", "per_launch_ms")
     out = {k: line[k] for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data")}
-    cfg = line["config"]
-    out["config"] = {"workload": cfg["workload"], "L": cfg["L"], "D": cfg["D"], "cutoff": cfg["cutoff"],
-                     "mpo": "compressed to bond dim 20", "update": "one-step Lanczos",
-                     "l2": "working set >> L2", "parallelism": cfg["parallelism"], "mode": cfg.get("mode")}
+    out["config"] = slim_config(line["config"])
     out["gpu_launches"] = line["gpu_launches"]
     out["clocks"] = {k: line["clocks"].get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")}
     def stages(r):  # {stage: [ms, Jacobi TFLOP/s, fraction of the stage's cuBLAS peak]}

@@ -91,3 +91,14 @@ def test_sig_rounds_floats_only():
     b = _bench()
     assert b.sig(3.14159265, 4) == 3.142
     assert b.sig({"a": [1.23456e-9, 7, "x"]}) == {"a": [1.235e-09, 7, "x"]}
+
+
+def test_both_arms_print_the_same_config():
+    """The reference arm and the GPU arm describe the cylinder workload identically."""
+    import types
+    b = _bench()
+    args = types.SimpleNamespace(D=2048, seed=0, ramp_sweeps=2, converge_sweeps=2, ramp_lanczos=4, warmup=3)
+    ours = dict(b.cylinder_config(args), parallelism="single GPU", mode="tf32x3")
+    ref = dict(b.cylinder_config(args), parallelism="single GPU")
+    assert b.slim_config(ours) == b.slim_config(ref)
+    assert b.slim_config(ours)["D"] == 2048
